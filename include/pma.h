@@ -1,0 +1,221 @@
+/*
+ * pma — GB300-native pore-throat and shortest-path pipeline (C ABI).
+ *
+ * Drop-in for the ImageProcessing services of PorousMediaAnalysis. Every volume-level
+ * entry point replaces one service method of the reference; the folder-level entry point
+ * replaces the command-line modes. No C++ exceptions cross this boundary: every call
+ * returns a pma_status and, on failure, pma_last_error() gives the message (the reference
+ * throws Core::InvalidOperationException and prints it in Main.cpp:62-98).
+ *
+ * Volumes are dense arrays in the reference's memory order [z][x][y] (y fastest,
+ * DataArray.h:85-94): x is the TIFF row, y the TIFF column, z the slice. Device pointers
+ * are plain CUDA device addresses on the context's device. Element types are those of
+ * ImageProcessing/Model/Headers/Types.h:16-25 (uint32 for squared distances, ids and
+ * coordinates; uint8 masks; float32 geodesics, plus a float64 variant).
+ *
+ * The total voxel count of one volume must stay below 2^32.
+ */
+#ifndef PMA_H
+#define PMA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PMA_ABI_VERSION 1
+
+typedef enum pma_status {
+    PMA_OK = 0,
+    PMA_ERR_ARGUMENT = 1,   /* bad size, null pointer, unsupported option */
+    PMA_ERR_CUDA = 2,       /* CUDA runtime error or missing device */
+    PMA_ERR_IO = 3,         /* file missing, unreadable or malformed */
+    PMA_ERR_MEMORY = 4,     /* device or host allocation failed, or budget exceeded */
+    PMA_ERR_LIMIT = 5,      /* a bounded device loop gave up (iteration limit reached) */
+    PMA_ERR_INTERNAL = 6
+} pma_status;
+
+typedef struct pma_dims {
+    int32_t sx, sy, sz;     /* X (rows), Y (columns), Z (slices) */
+} pma_dims;
+
+/* Stencil of pore propagation, watershed and geodesics ("Use D3Q7 stencil", Config.h:39). */
+typedef enum pma_stencil { PMA_D3Q27 = 0, PMA_D3Q7 = 1 } pma_stencil;
+
+/* Copies the calling thread's last error message into buf; returns its full length. */
+size_t pma_last_error(char* buf, size_t cap);
+int pma_abi_version(void);
+
+/* ---------------------------------------------------------------------------------
+ * Context: one device, one CUDA stream, cached device scratch memory.
+ * ------------------------------------------------------------------------------- */
+typedef struct pma_ctx pma_ctx;
+int pma_ctx_create(int device, pma_ctx** out);
+int pma_ctx_destroy(pma_ctx* ctx);
+/* Runs subsequent work of ctx on an existing cudaStream_t (NULL = the context's own). */
+int pma_ctx_set_stream(pma_ctx* ctx, void* cuda_stream);
+/* Number of this library's kernels launched through ctx since creation. */
+uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
+/* Device bytes held by ctx's scratch cache; pma_ctx_trim releases them. */
+size_t pma_ctx_scratch_bytes(const pma_ctx* ctx);
+int pma_ctx_trim(pma_ctx* ctx);
+
+/* ---------------------------------------------------------------------------------
+ * Stage entry points on device buffers. All run on the context's stream and return
+ * after the stream work they need on the host has completed.
+ * ------------------------------------------------------------------------------- */
+
+typedef struct pma_edt_stats {
+    uint32_t max_edt2;          /* "Max Euclidean distance square" */
+    uint32_t pad_;
+    uint64_t hist_len;          /* max_edt2 + 1 */
+} pma_edt_stats;
+
+/* Squared Euclidean distance transform, its maximum and the histogram of balls that do
+ * not cross the image boundary. Replaces EuclideanDistanceComputer::ComputeEuclideanDistances
+ * (EuclideanDistanceComputer.cpp:30-44; passes :149-343). d_solid: non-zero = solid.
+ * h_hist (host, may be NULL) receives min(hist_cap, max_edt2+1) counters. */
+int pma_edt(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, uint32_t* d_edt2,
+            pma_edt_stats* stats, uint64_t* h_hist, size_t hist_cap);
+
+/* Containing-ball radii (squared), the winning centre of each void voxel and the
+ * IsMaximumBall mask (0 solid, 127 inner, 255 outer). Replaces
+ * ContainingBallsAssigner::SetContainingBalls (ContainingBallsAssigner.cpp:36-60;
+ * scatter :101-183, mask :190-250) with its single-thread tie rule: the winner is the
+ * lexicographically smallest (x, y, z) centre among those of maximal radius. */
+int pma_containing_balls(pma_ctx* ctx, const uint32_t* d_edt2, pma_dims dims, uint32_t max_edt2,
+                         uint32_t* d_crad2, uint32_t* d_cx, uint32_t* d_cy, uint32_t* d_cz,
+                         uint8_t* d_maxball_mask, uint64_t* h_maximum_balls_count);
+
+/* Pores and throats table (host memory, owned by the library). */
+typedef struct pma_pore {       /* a row of pores.txt (Serializer.cpp:187-201) */
+    uint32_t id;
+    int32_t seed_x, seed_y, seed_z;
+    uint32_t seed_r2;
+    int32_t is_boundary;
+    uint64_t volume;
+} pma_pore;
+
+typedef struct pma_throat {     /* a row of sharedPixelTypes.txt (Serializer.cpp:203-221) */
+    uint32_t id;
+    uint32_t n_pores;
+    uint64_t volume;
+    uint64_t pool_offset;       /* pore ids at pool[pool_offset .. pool_offset + n_pores) */
+} pma_throat;
+
+typedef struct pma_table pma_table;
+int pma_table_create(const pma_pore* pores, size_t n_pores, const pma_throat* throats,
+                     size_t n_throats, const uint32_t* pool, size_t pool_size, pma_table** out);
+size_t pma_table_npores(const pma_table* t);
+const pma_pore* pma_table_pores(const pma_table* t);
+size_t pma_table_nthroats(const pma_table* t);
+const pma_throat* pma_table_throats(const pma_table* t);
+size_t pma_table_pool_size(const pma_table* t);
+const uint32_t* pma_table_pool(const pma_table* t);
+void pma_table_free(pma_table* t);
+
+/* Pore seeds and the initial pore propagation: replaces
+ * PoreAndThroatComputer::AssignPoreAndThroatIds (PoreAndThroatComputer.cpp:35-55; seeds
+ * :93-163, propagation :192-269, pixel states BasePoreAndThroatComputer.cpp:37-133).
+ * Pore ids, seeds, radii, volumes, boundary flags and every voxel's pore set are exact.
+ * Throat ids are numbered in a breadth-first creation order; the reference numbers them
+ * in its depth-first creation order, so throat ids match it up to a one-to-one renaming.
+ * d_labels is written completely. */
+int pma_pores(pma_ctx* ctx, const uint8_t* d_maxball_mask, const uint32_t* d_edt2,
+              const uint32_t* d_crad2, pma_dims dims, pma_stencil stencil, uint32_t* d_labels,
+              pma_table** out);
+
+/* Drops zero-volume pores, merges and renames throats and remaps d_labels. Replaces
+ * EmptyPoresRemover::RemoveEmptyPores (EmptyPoresRemover.cpp:31-244). */
+int pma_remove_empty_pores(pma_ctx* ctx, pma_table* table, uint32_t* d_labels, pma_dims dims);
+
+/* Watershed labelling from the pores of `pores`. Replaces
+ * WatershedComputer::AssignPoreAndThroatIds (WatershedComputer.cpp:30-219), bit-exact
+ * including throat ids. d_labels_ws is written completely. */
+int pma_watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* d_crad2, pma_dims dims,
+                  pma_stencil stencil, uint32_t max_edt2, uint32_t* d_labels_ws, pma_table** out);
+
+typedef struct pma_cavity {     /* a row of cavityDescriptions.txt (Serializer.cpp:161-185) */
+    uint32_t id;
+    int32_t seed_x, seed_y, seed_z;
+    float distance_to_center;
+    int32_t reached_walls;
+    uint64_t void_count;
+    int32_t reaches_all_walls;
+    int32_t pad_;
+} pma_cavity;
+
+/* Geodesic distances from the void voxel nearest the centre, cavity restarts and cavity
+ * ids. Replaces ShortestPathComputer::ComputeShortestPathDistances
+ * (ShortestPathComputer.cpp:39-511). Distances: -1 solid, FLT_MAX (DBL_MAX) unreached;
+ * cavity ids: 0 solid, UINT32_MAX unreached. The f32 variant is bit-exact with the
+ * reference; the f64 variant accumulates the same steps in double precision. */
+int pma_geodesic_f32(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_stencil stencil,
+                     float* d_dist, uint32_t* d_cavity, pma_cavity* h_cavities, int cavity_cap,
+                     int* n_cavities);
+int pma_geodesic_f64(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_stencil stencil,
+                     double* d_dist, uint32_t* d_cavity, pma_cavity* h_cavities, int cavity_cap,
+                     int* n_cavities);
+
+/* ---------------------------------------------------------------------------------
+ * Whole pipeline on one volume, host buffers in and out (EDT -> containing balls ->
+ * pores -> empty-pore removal -> watershed, plus geodesics), the host<->device copies
+ * included. Any output pointer may be NULL to skip copying that field back.
+ * ------------------------------------------------------------------------------- */
+typedef struct pma_outputs {
+    uint32_t* edt2;             /* EuclideanDistanceSquares */
+    uint32_t* crad2;            /* ContainingBallRadiiSquares */
+    uint32_t* cx; uint32_t* cy; uint32_t* cz;   /* ContainingBallCoordinatesX/Y/Z */
+    uint8_t* maxball_mask;      /* IsMaximumBall */
+    uint32_t* pore_labels;      /* PoreThroatIds (after empty-pore removal) */
+    uint32_t* watershed_labels; /* PoreThroatIdsWatershed */
+    float* dist_f32;            /* ShortestPathDistances, float32 */
+    double* dist_f64;           /* geodesics in float64 (computed only when non-NULL) */
+    uint32_t* cavity;           /* CavityIds */
+    /* results filled by the call */
+    pma_edt_stats edt_stats;
+    uint64_t maximum_balls_count;
+    pma_table* pores;           /* after empty-pore removal (caller frees) */
+    pma_table* watershed;       /* watershed pores and throats (caller frees) */
+    pma_cavity cavities[16];
+    int n_cavities;
+    int pad_;
+} pma_outputs;
+
+typedef struct pma_options {
+    pma_stencil stencil;
+    int run_pores;              /* 1: EDT..watershed */
+    int run_geodesic;           /* 1: geodesics */
+    int pad_;
+} pma_options;
+
+int pma_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims,
+                      const pma_options* opts, pma_outputs* out);
+
+/* ---------------------------------------------------------------------------------
+ * Folder-level drop-in for the command-line modes (CommandLineDispatcher.cpp:34-72,
+ * ImageProcessingManager.cpp:63-108): walks every folder under base_folder holding a
+ * config.txt, reads Images/ and writes the same TIFF folders and text files.
+ * ------------------------------------------------------------------------------- */
+typedef enum pma_mode {
+    PMA_MODE_ALL = 1, PMA_MODE_EDT = 2, PMA_MODE_RIB = 3, PMA_MODE_APT = 4, PMA_MODE_SPD = 5
+} pma_mode;
+
+int pma_run_folder(pma_ctx* ctx, const char* base_folder, pma_mode mode);
+
+/* ---------------------------------------------------------------------------------
+ * Host I/O (no GPU needed).
+ * ------------------------------------------------------------------------------- */
+/* Reads a TIFF stack folder (slices sorted by name) of 1- or 4-byte voxels into
+ * [z][x][y]. With out == NULL only dims are filled. */
+int pma_read_tiff_stack(const char* folder, int bytes_per_voxel, pma_dims* dims, void* out,
+                        size_t out_bytes);
+/* Writes [z][x][y] voxels as slices 1.tif .. SZ.tif (8-bit grey or 32-bit CMYK LZW). */
+int pma_write_tiff_stack(const char* folder, int bytes_per_voxel, pma_dims dims, const void* data);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMA_H */

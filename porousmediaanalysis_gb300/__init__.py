@@ -1,0 +1,215 @@
+"""GB300-native pore-throat and shortest-path pipeline (PorousMediaAnalysis drop-in).
+
+The compute path is libpma.so: hand-written CUDA kernels for sm_103a behind the C ABI of
+include/pma.h. This module wraps that ABI for torch CUDA tensors; torch only provides the
+device memory and the stream. Volumes are (SZ, SX, SY) tensors, the reference's [z][x][y]
+memory order; uint32 fields are carried in int32 tensors with the same bits.
+
+Stage functions mirror the reference services:
+    compute_euclidean_distances   EuclideanDistanceComputer::ComputeEuclideanDistances
+    set_containing_balls          ContainingBallsAssigner::SetContainingBalls
+    assign_pore_and_throat_ids    PoreAndThroatComputer::AssignPoreAndThroatIds
+    remove_empty_pores            EmptyPoresRemover::RemoveEmptyPores
+    assign_watershed_ids          WatershedComputer::AssignPoreAndThroatIds
+    compute_shortest_path_distances ShortestPathComputer::ComputeShortestPathDistances
+    run_folder                    the -all/-edt/-rib/-apt/-spd command-line modes
+"""
+import ctypes
+
+from . import capi
+from .capi import D3Q7, D3Q27, MODE_ALL, MODE_APT, MODE_EDT, MODE_RIB, MODE_SPD, PmaError
+
+__all__ = ["Context", "Table", "compute_euclidean_distances", "set_containing_balls",
+           "assign_pore_and_throat_ids", "remove_empty_pores", "assign_watershed_ids",
+           "compute_shortest_path_distances", "run_folder", "pipeline_host", "D3Q7", "D3Q27",
+           "MODE_ALL", "MODE_EDT", "MODE_RIB", "MODE_APT", "MODE_SPD", "PmaError"]
+
+
+class Context:
+    """One pma_ctx: a device, a stream (torch's current stream) and cached scratch."""
+
+    def __init__(self, device=0, stream=None):
+        import torch
+        self.device = device
+        h = ctypes.c_void_p()
+        capi.check(capi.lib().pma_ctx_create(device, ctypes.byref(h)))
+        self.handle = h
+        if stream is None:
+            stream = torch.cuda.current_stream(device)
+        self.stream = stream
+        capi.check(capi.lib().pma_ctx_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+
+    def close(self):
+        if self.handle:
+            capi.lib().pma_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launch_count(self):
+        return capi.lib().pma_ctx_launch_count(self.handle)
+
+    @property
+    def scratch_bytes(self):
+        return capi.lib().pma_ctx_scratch_bytes(self.handle)
+
+
+class Table:
+    """Owning wrapper of a pma_table (pores + throats)."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    @classmethod
+    def from_rows(cls, pores, throats=()):
+        pa = (capi.Pore * max(1, len(pores)))()
+        for i, p in enumerate(pores):
+            pa[i] = capi.Pore(*p)
+        pool = []
+        ta = (capi.Throat * max(1, len(throats)))()
+        for i, (tid, vol, plist) in enumerate(throats):
+            ta[i] = capi.Throat(tid, len(plist), vol, len(pool))
+            pool.extend(plist)
+        pl = (ctypes.c_uint32 * max(1, len(pool)))(*pool)
+        h = ctypes.c_void_p()
+        capi.check(capi.lib().pma_table_create(pa, len(pores), ta, len(throats), pl, len(pool),
+                                               ctypes.byref(h)))
+        return cls(h)
+
+    def rows(self):
+        return capi.table_to_python(self.handle)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            capi.lib().pma_table_free(self.handle)
+            self.handle = None
+
+
+def _dims(t):
+    sz, sx, sy = t.shape
+    return capi.Dims(sx, sy, sz)
+
+
+def _ptr(t):
+    assert t.is_cuda and t.is_contiguous()
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def compute_euclidean_distances(ctx, solid, hist_cap=0):
+    """Squared EDT of a (SZ, SX, SY) uint8 CUDA tensor (non-zero = solid).
+    Returns (edt2 int32 tensor, max_edt2, histogram list)."""
+    import torch
+    edt2 = torch.empty(solid.shape, dtype=torch.int32, device=solid.device)
+    st = capi.EdtStats()
+    hist = (ctypes.c_uint64 * max(1, hist_cap))()
+    capi.check(capi.lib().pma_edt(ctx.handle, _ptr(solid), _dims(solid), _ptr(edt2),
+                                  ctypes.byref(st), hist if hist_cap else None, hist_cap))
+    n = min(hist_cap, st.max_edt2 + 1)
+    return edt2, st.max_edt2, [hist[i] for i in range(n)]
+
+
+def set_containing_balls(ctx, edt2, max_edt2):
+    """Returns (crad2, cx, cy, cz, maxball_mask, maximum_balls_count)."""
+    import torch
+    dev = edt2.device
+    crad2 = torch.empty(edt2.shape, dtype=torch.int32, device=dev)
+    cx = torch.empty_like(crad2)
+    cy = torch.empty_like(crad2)
+    cz = torch.empty_like(crad2)
+    mask = torch.empty(edt2.shape, dtype=torch.uint8, device=dev)
+    count = ctypes.c_uint64()
+    capi.check(capi.lib().pma_containing_balls(ctx.handle, _ptr(edt2), _dims(edt2), max_edt2,
+                                               _ptr(crad2), _ptr(cx), _ptr(cy), _ptr(cz),
+                                               _ptr(mask), ctypes.byref(count)))
+    return crad2, cx, cy, cz, mask, count.value
+
+
+def assign_pore_and_throat_ids(ctx, mask, edt2, crad2, stencil=D3Q27):
+    """Returns (labels int32 tensor, Table)."""
+    import torch
+    labels = torch.empty(edt2.shape, dtype=torch.int32, device=edt2.device)
+    h = ctypes.c_void_p()
+    capi.check(capi.lib().pma_pores(ctx.handle, _ptr(mask), _ptr(edt2), _ptr(crad2), _dims(edt2),
+                                    stencil, _ptr(labels), ctypes.byref(h)))
+    return labels, Table(h)
+
+
+def remove_empty_pores(ctx, table, labels):
+    capi.check(capi.lib().pma_remove_empty_pores(ctx.handle, table.handle, _ptr(labels),
+                                                 _dims(labels)))
+
+
+def assign_watershed_ids(ctx, table, crad2, max_edt2, stencil=D3Q27):
+    """Returns (watershed labels int32 tensor, Table)."""
+    import torch
+    labels = torch.empty(crad2.shape, dtype=torch.int32, device=crad2.device)
+    h = ctypes.c_void_p()
+    capi.check(capi.lib().pma_watershed(ctx.handle, table.handle, _ptr(crad2), _dims(crad2),
+                                        stencil, max_edt2, _ptr(labels), ctypes.byref(h)))
+    return labels, Table(h)
+
+
+def compute_shortest_path_distances(ctx, solid, stencil=D3Q27, fp64=False):
+    """Returns (dist float32/float64 tensor, cavity int32 tensor, cavity rows)."""
+    import torch
+    dist = torch.empty(solid.shape, dtype=torch.float64 if fp64 else torch.float32,
+                       device=solid.device)
+    cav = torch.empty(solid.shape, dtype=torch.int32, device=solid.device)
+    rows = (capi.Cavity * 64)()
+    n = ctypes.c_int()
+    fn = capi.lib().pma_geodesic_f64 if fp64 else capi.lib().pma_geodesic_f32
+    capi.check(fn(ctx.handle, _ptr(solid), _dims(solid), stencil, _ptr(dist), _ptr(cav), rows, 64,
+                  ctypes.byref(n)))
+    out = [(r.id, r.seed_x, r.seed_y, r.seed_z, r.distance_to_center, r.void_count,
+            r.reached_walls, r.reaches_all_walls) for r in rows[:n.value]]
+    return dist, cav, out
+
+
+def run_folder(ctx, base_folder, mode=MODE_ALL):
+    capi.check(capi.lib().pma_run_folder(ctx.handle, str(base_folder).encode(), mode))
+
+
+def pipeline_host(ctx, solid_np, stencil=D3Q27, run_pores=True, run_geodesic=True, fp64=False,
+                  fields=("watershed_labels", "dist_f32")):
+    """Whole pipeline on a host (SZ, SX, SY) uint8 numpy array (pinned copies inside).
+    Returns a dict of numpy outputs for `fields`, plus tables and statistics."""
+    import numpy as np
+    solid_np = np.ascontiguousarray(solid_np, dtype=np.uint8)
+    out = capi.Outputs()
+    res = {}
+    kinds = {"edt2": np.uint32, "crad2": np.uint32, "cx": np.uint32, "cy": np.uint32,
+             "cz": np.uint32, "maxball_mask": np.uint8, "pore_labels": np.uint32,
+             "watershed_labels": np.uint32, "dist_f32": np.float32, "dist_f64": np.float64,
+             "cavity": np.uint32}
+    for name in fields:
+        arr = np.empty(solid_np.shape, dtype=kinds[name])
+        res[name] = arr
+        ctype = type(getattr(out, name))
+        setattr(out, name, ctypes.cast(arr.ctypes.data, ctype))
+    if fp64 and "dist_f64" not in res:
+        arr = np.empty(solid_np.shape, dtype=np.float64)
+        res["dist_f64"] = arr
+        out.dist_f64 = ctypes.cast(arr.ctypes.data, ctypes.POINTER(ctypes.c_double))
+    opts = capi.Options(stencil, int(run_pores), int(run_geodesic), 0)
+    capi.check(capi.lib().pma_pipeline_host(ctx.handle, solid_np.ctypes.data, capi.Dims(
+        solid_np.shape[1], solid_np.shape[2], solid_np.shape[0]), ctypes.byref(opts),
+        ctypes.byref(out)))
+    res["max_edt2"] = out.edt_stats.max_edt2
+    res["maximum_balls_count"] = out.maximum_balls_count
+    res["pores"] = Table(out.pores) if out.pores else None
+    res["watershed"] = Table(out.watershed) if out.watershed else None
+    res["cavities"] = [(c.id, c.seed_x, c.seed_y, c.seed_z, c.distance_to_center, c.void_count,
+                        c.reached_walls, c.reaches_all_walls)
+                       for c in out.cavities[:out.n_cavities]]
+    return res

@@ -1,0 +1,264 @@
+// C ABI of the pma library (include/pma.h): context, errors, tables and stage wrappers.
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "pma_internal.h"
+#include "pma_io.h"
+
+namespace pma {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+}  // namespace pma
+
+using pma::Error;
+using pma::guarded;
+
+void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
+    Buf& b = cache[tag];
+    if (b.bytes >= bytes && b.ptr) return b.ptr;
+    if (b.ptr) {
+        PMA_CUDA(cudaStreamSynchronize(stream));
+        PMA_CUDA(cudaFree(b.ptr));
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&b.ptr, want);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        (void)cudaGetLastError();
+        throw Error(PMA_ERR_MEMORY, "device allocation of " + std::to_string(want) + " bytes for " +
+                                        tag + " failed: " + cudaGetErrorString(e));
+    }
+    b.bytes = want;
+    return b.ptr;
+}
+
+void* pma_ctx::host_staging(size_t bytes) {
+    if (pinned_bytes >= bytes && pinned) return pinned;
+    if (pinned) {
+        PMA_CUDA(cudaStreamSynchronize(stream));
+        PMA_CUDA(cudaFreeHost(pinned));
+        pinned = nullptr;
+    }
+    PMA_CUDA(cudaMallocHost(&pinned, bytes));
+    pinned_bytes = bytes;
+    return pinned;
+}
+
+void pma_ctx::sync() { PMA_CUDA(cudaStreamSynchronize(stream)); }
+
+void pma_ctx::check_launch(const char* what) {
+    count_launch(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(PMA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+extern "C" {
+
+size_t pma_last_error(char* buf, size_t cap) {
+    const std::string& m = pma::g_last_error;
+    if (buf && cap) {
+        size_t n = std::min(cap - 1, m.size());
+        std::memcpy(buf, m.data(), n);
+        buf[n] = 0;
+    }
+    return m.size();
+}
+
+int pma_abi_version(void) { return PMA_ABI_VERSION; }
+
+int pma_ctx_create(int device, pma_ctx** out) {
+    return guarded([&] {
+        PMA_REQUIRE(out, PMA_ERR_ARGUMENT, "pma_ctx_create: null output");
+        int n = 0;
+        PMA_CUDA(cudaGetDeviceCount(&n));
+        PMA_REQUIRE(device >= 0 && device < n, PMA_ERR_CUDA, "pma_ctx_create: no such CUDA device");
+        PMA_CUDA(cudaSetDevice(device));
+        pma_ctx* c = new pma_ctx;
+        c->device = device;
+        cudaDeviceProp p;
+        PMA_CUDA(cudaGetDeviceProperties(&p, device));
+        c->num_sms = p.multiProcessorCount;
+        c->smem_optin = p.sharedMemPerBlockOptin;
+        PMA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+        *out = c;
+    });
+}
+
+int pma_ctx_destroy(pma_ctx* ctx) {
+    if (!ctx) return PMA_OK;
+    return guarded([&] {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        for (auto& kv : ctx->cache)
+            if (kv.second.ptr) cudaFree(kv.second.ptr);
+        if (ctx->pinned) cudaFreeHost(ctx->pinned);
+        if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+    });
+}
+
+int pma_ctx_set_stream(pma_ctx* ctx, void* stream) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        if (ctx->own_stream) {
+            PMA_CUDA(cudaStreamSynchronize(ctx->stream));
+            PMA_CUDA(cudaStreamDestroy(ctx->stream));
+            ctx->own_stream = false;
+        }
+        if (stream) {
+            ctx->stream = static_cast<cudaStream_t>(stream);
+        } else {
+            PMA_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+            ctx->own_stream = true;
+        }
+    });
+}
+
+uint64_t pma_ctx_launch_count(const pma_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
+
+size_t pma_ctx_scratch_bytes(const pma_ctx* ctx) {
+    size_t s = 0;
+    if (ctx)
+        for (auto& kv : ctx->cache) s += kv.second.bytes;
+    return s;
+}
+
+int pma_ctx_trim(pma_ctx* ctx) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        PMA_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (auto& kv : ctx->cache)
+            if (kv.second.ptr) PMA_CUDA(cudaFree(kv.second.ptr));
+        ctx->cache.clear();
+    });
+}
+
+int pma_edt(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, uint32_t* d_edt2,
+            pma_edt_stats* stats, uint64_t* h_hist, size_t hist_cap) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        pma::edt(ctx, d_solid, dims, d_edt2, stats, h_hist, hist_cap);
+    });
+}
+
+int pma_containing_balls(pma_ctx* ctx, const uint32_t* d_edt2, pma_dims dims, uint32_t max_edt2,
+                         uint32_t* d_crad2, uint32_t* d_cx, uint32_t* d_cy, uint32_t* d_cz,
+                         uint8_t* d_mask, uint64_t* h_count) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        pma::containing_balls(ctx, d_edt2, dims, max_edt2, d_crad2, d_cx, d_cy, d_cz, d_mask, h_count);
+    });
+}
+
+int pma_table_create(const pma_pore* pores, size_t n_pores, const pma_throat* throats,
+                     size_t n_throats, const uint32_t* pool, size_t pool_size, pma_table** out) {
+    return guarded([&] {
+        PMA_REQUIRE(out, PMA_ERR_ARGUMENT, "pma_table_create: null output");
+        PMA_REQUIRE(n_pores == 0 || pores, PMA_ERR_ARGUMENT, "pma_table_create: null pores");
+        PMA_REQUIRE(n_throats == 0 || throats, PMA_ERR_ARGUMENT, "pma_table_create: null throats");
+        PMA_REQUIRE(pool_size == 0 || pool, PMA_ERR_ARGUMENT, "pma_table_create: null pool");
+        for (size_t i = 0; i < n_throats; ++i)
+            PMA_REQUIRE(throats[i].pool_offset + throats[i].n_pores <= pool_size, PMA_ERR_ARGUMENT,
+                        "pma_table_create: throat pore list outside the pool");
+        pma_table* t = new pma_table;
+        t->pores.assign(pores, pores + n_pores);
+        t->throats.assign(throats, throats + n_throats);
+        t->pool.assign(pool, pool + pool_size);
+        *out = t;
+    });
+}
+
+size_t pma_table_npores(const pma_table* t) { return t ? t->pores.size() : 0; }
+const pma_pore* pma_table_pores(const pma_table* t) { return t ? t->pores.data() : nullptr; }
+size_t pma_table_nthroats(const pma_table* t) { return t ? t->throats.size() : 0; }
+const pma_throat* pma_table_throats(const pma_table* t) { return t ? t->throats.data() : nullptr; }
+size_t pma_table_pool_size(const pma_table* t) { return t ? t->pool.size() : 0; }
+const uint32_t* pma_table_pool(const pma_table* t) { return t ? t->pool.data() : nullptr; }
+void pma_table_free(pma_table* t) { delete t; }
+
+int pma_pores(pma_ctx* ctx, const uint8_t* d_mask, const uint32_t* d_edt2, const uint32_t* d_crad2,
+              pma_dims dims, pma_stencil stencil, uint32_t* d_labels, pma_table** out) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx && out, PMA_ERR_ARGUMENT, "pma_pores: null context or output");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        *out = pma::pores(ctx, d_mask, d_edt2, d_crad2, dims, stencil, d_labels);
+    });
+}
+
+int pma_remove_empty_pores(pma_ctx* ctx, pma_table* table, uint32_t* d_labels, pma_dims dims) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx && table, PMA_ERR_ARGUMENT, "pma_remove_empty_pores: null context or table");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        pma::remove_empty_pores(ctx, table, d_labels, dims);
+    });
+}
+
+int pma_watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* d_crad2, pma_dims dims,
+                  pma_stencil stencil, uint32_t max_edt2, uint32_t* d_labels_ws, pma_table** out) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx && pores && out, PMA_ERR_ARGUMENT, "pma_watershed: null argument");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        *out = pma::watershed(ctx, pores, d_crad2, dims, stencil, max_edt2, d_labels_ws);
+    });
+}
+
+int pma_geodesic_f32(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_stencil stencil,
+                     float* d_dist, uint32_t* d_cavity, pma_cavity* h_cav, int cap, int* n_cav) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        int n = pma::geodesic<float>(ctx, d_solid, dims, stencil, d_dist, d_cavity, h_cav, cap);
+        if (n_cav) *n_cav = n;
+    });
+}
+
+int pma_geodesic_f64(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_stencil stencil,
+                     double* d_dist, uint32_t* d_cavity, pma_cavity* h_cav, int cap, int* n_cav) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        int n = pma::geodesic<double>(ctx, d_solid, dims, stencil, d_dist, d_cavity, h_cav, cap);
+        if (n_cav) *n_cav = n;
+    });
+}
+
+int pma_read_tiff_stack(const char* folder, int bpv, pma_dims* dims, void* out, size_t out_bytes) {
+    return guarded([&] {
+        PMA_REQUIRE(folder && dims, PMA_ERR_ARGUMENT, "pma_read_tiff_stack: null argument");
+        PMA_REQUIRE(bpv == 1 || bpv == 4, PMA_ERR_ARGUMENT, "pma_read_tiff_stack: 1 or 4 bytes per voxel");
+        pma::Dims d;
+        std::vector<uint8_t> v = pma::read_stack(folder, bpv, &d);
+        dims->sx = d.sx;
+        dims->sy = d.sy;
+        dims->sz = d.sz;
+        if (out) {
+            PMA_REQUIRE(out_bytes >= v.size(), PMA_ERR_ARGUMENT, "pma_read_tiff_stack: output too small");
+            std::memcpy(out, v.data(), v.size());
+        }
+    });
+}
+
+int pma_write_tiff_stack(const char* folder, int bpv, pma_dims dims, const void* data) {
+    return guarded([&] {
+        PMA_REQUIRE(folder && data, PMA_ERR_ARGUMENT, "pma_write_tiff_stack: null argument");
+        PMA_REQUIRE(bpv == 1 || bpv == 4, PMA_ERR_ARGUMENT, "pma_write_tiff_stack: 1 or 4 bytes per voxel");
+        pma::Dims d;
+        d.sx = dims.sx;
+        d.sy = dims.sy;
+        d.sz = dims.sz;
+        pma::write_stack(folder, {}, data, bpv, d);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,335 @@
+// Geodesic (shortest-path) distances, cavity ids and cavity restarts
+// (ShortestPathComputer.cpp:39-511).
+//
+// The reference settles voxels with Dijkstra over an indexed heap (HeapUtilities.h).
+// Every settled distance equals min over void neighbours u of fl(d(u) + w(u, v)); this
+// system has one greatest fixed point below the initial values and any monotone
+// relaxation that runs until nothing improves reaches it, so the parallel form below is
+// bit-identical in float32 (and in float64 against the float64 restatement).
+//
+// Bucketing: all step weights w are >= 1 (1, sqrt 2, sqrt 3, or 1 for D3Q7) and in
+// round-to-nearest fl(d + w) >= floor(d) + 1, so relaxing a voxel of bucket floor(d) = k
+// only reaches buckets k+1 and k+2. Bucket k is therefore final when it is processed and
+// one parallel sweep per bucket suffices (Dial's algorithm). Buckets live in a ring of
+// four voxel lists; a per-voxel mark keeps a voxel at most once in each bucket list.
+#include "pma_internal.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+namespace pma {
+namespace {
+
+template <class T> struct Bits;
+template <> struct Bits<float> {
+    typedef unsigned int U;
+    static __device__ __forceinline__ U to(float f) { return __float_as_uint(f); }
+    static __device__ __forceinline__ float from(U u) { return __uint_as_float(u); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __host__ __device__ float unknown() { return FLT_MAX; }
+    static __device__ __forceinline__ int bucket(float d) { return static_cast<int>(floorf(d)); }
+};
+template <> struct Bits<double> {
+    typedef unsigned long long U;
+    static __device__ __forceinline__ U to(double f) { return static_cast<U>(__double_as_longlong(f)); }
+    static __device__ __forceinline__ double from(U u) { return __longlong_as_double(static_cast<long long>(u)); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __host__ __device__ double unknown() { return DBL_MAX; }
+    static __device__ __forceinline__ int bucket(double d) { return static_cast<int>(floor(d)); }
+};
+
+struct Geo {
+    int SX, SY, SZ;
+    __device__ __forceinline__ size_t idx(int x, int y, int z) const {
+        return (static_cast<size_t>(z) * SX + x) * SY + y;
+    }
+};
+
+struct Frontier {
+    uint32_t* list[4];
+    unsigned int* count;   // [4]
+    uint32_t cap;
+    unsigned int* overflow;
+    unsigned long long* settled;  // voxels settled in this cavity
+    unsigned int* walls;          // bit 2i: plane axis i at 0, bit 2i+1: at size-1
+};
+
+template <class T>
+__global__ void geo_init(const uint8_t* __restrict__ solid, size_t n, T* __restrict__ dist,
+                         uint32_t* __restrict__ cavity, int* __restrict__ mark) {
+    for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
+         v += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const bool s = solid[v] != 0;  // SPC.cpp:354-372
+        dist[v] = s ? static_cast<T>(-1) : Bits<T>::unknown();
+        cavity[v] = s ? 0u : 0xFFFFFFFFu;
+        mark[v] = -1;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void enqueue(const Frontier& f, int* mark, uint32_t v, T d) {
+    const int b = Bits<T>::bucket(d);
+    if (atomicExch(&mark[v], b) == b) return;
+    const unsigned pos = atomicAdd(&f.count[b & 3], 1u);
+    if (pos < f.cap) f.list[b & 3][pos] = v;
+    else atomicExch(f.overflow, 1u);
+}
+
+template <class T>
+__global__ void geo_start(Frontier f, int* mark, T* dist, uint32_t v) {
+    dist[v] = static_cast<T>(0);
+    enqueue<T>(f, mark, v, static_cast<T>(0));
+}
+
+// Processes bucket k: settle its voxels and relax their neighbours.
+template <class T>
+__global__ void geo_bucket(const uint8_t* __restrict__ solid, Geo g, int d3q7, T w1, T w2, T w3,
+                           T* __restrict__ dist, uint32_t* __restrict__ cavity, int* __restrict__ mark,
+                           Frontier f, int k, uint32_t cavity_id) {
+    typedef typename Bits<T>::U U;
+    if (blockIdx.x == 0 && threadIdx.x == 0) f.count[(k + 3) & 3] = 0;  // list of bucket k-1
+    const unsigned n = min(f.count[k & 3], f.cap);
+    const uint32_t* list = f.list[k & 3];
+    unsigned long long my_settled = 0;
+    unsigned my_walls = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = list[i];
+        const T dv = dist[v];
+        if (Bits<T>::bucket(dv) != k) continue;  // stale entry
+        if (cavity[v] == cavity_id) continue;                                  // duplicate
+        cavity[v] = cavity_id;
+        ++my_settled;
+        const int y = static_cast<int>(v % g.SY);
+        const uint32_t zx = v / g.SY;
+        const int x = static_cast<int>(zx % g.SX);
+        const int z = static_cast<int>(zx / g.SX);
+        if (x == 0) my_walls |= 1u;
+        if (x == g.SX - 1 && g.SX > 1) my_walls |= 2u;
+        if (y == 0) my_walls |= 4u;
+        if (y == g.SY - 1 && g.SY > 1) my_walls |= 8u;
+        if (z == 0) my_walls |= 16u;
+        if (z == g.SZ - 1 && g.SZ > 1) my_walls |= 32u;
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int nx = x + dx;
+            if (nx < 0 || nx >= g.SX) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int ny = y + dy;
+                if (ny < 0 || ny >= g.SY) continue;
+                for (int dz = -1; dz <= 1; ++dz) {
+                    const int nz = z + dz;
+                    if (nz < 0 || nz >= g.SZ) continue;
+                    const int kk = dx * dx + dy * dy + dz * dz;
+                    if (kk == 0) continue;
+                    if (d3q7 && kk > 1) continue;
+                    const size_t w = g.idx(nx, ny, nz);
+                    if (solid[w] != 0) continue;
+                    const T step = d3q7 ? static_cast<T>(1) : (kk == 1 ? w1 : (kk == 2 ? w2 : w3));
+                    const T nd = Bits<T>::add(dv, step);
+                    if (!(nd < dist[w])) continue;
+                    const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
+                    if (Bits<T>::to(nd) < old) enqueue<T>(f, mark, static_cast<uint32_t>(w), nd);
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        my_settled += __shfl_xor_sync(0xFFFFFFFFu, my_settled, o);
+        my_walls |= __shfl_xor_sync(0xFFFFFFFFu, my_walls, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (my_settled) atomicAdd(f.settled, my_settled);
+        if (my_walls) atomicOr(f.walls, my_walls);
+    }
+}
+
+// Start-voxel search on box shells h0 .. h0+nh-1 around the centre, in the reference's
+// visiting order (SPC.cpp:460-511). Writes the smallest (shell, order) key of a void,
+// unreached voxel.
+template <class T>
+__global__ void geo_shell_search(const uint8_t* __restrict__ solid, const T* __restrict__ dist,
+                                 Geo g, int cx, int cy, int cz, int h0, int nh,
+                                 unsigned long long* __restrict__ best) {
+    const int s[3] = {g.SX, g.SY, g.SZ};
+    const int c[3] = {cx, cy, cz};
+    const int h = h0 + blockIdx.y;
+    if (blockIdx.y >= nh) return;
+    // segment sizes in order (k, f)
+    unsigned long long off = 0;
+    unsigned long long t = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+    for (int k = 0; k < 3; ++k) {
+        const int a = (k == 0) ? 1 : 0, b = (k == 2) ? 1 : 2;
+        const int a0 = max(c[a] - h, 0), a1 = min(c[a] + h, s[a] - 1);
+        const int b0 = max(c[b] - h, 0), b1 = min(c[b] + h, s[b] - 1);
+        const int f0 = max(c[k] - h, 0), f1 = min(c[k] + h, s[k] - 1);
+        const int nf = (f0 == f1) ? 1 : 2;
+        const unsigned long long na = a1 - a0 + 1, nb = b1 - b0 + 1;
+        const unsigned long long seg = static_cast<unsigned long long>(nf) * na * nb;
+        for (unsigned long long i = t; i < seg; i += gridDim.x * static_cast<unsigned long long>(blockDim.x)) {
+            const int f = static_cast<int>(i / (na * nb));
+            const unsigned long long r = i % (na * nb);
+            int p[3];
+            p[a] = a0 + static_cast<int>(r / nb);
+            p[b] = b0 + static_cast<int>(r % nb);
+            p[k] = f == 0 ? f0 : f1;
+            const size_t v = g.idx(p[0], p[1], p[2]);
+            if (solid[v] == 0 && dist[v] == Bits<T>::unknown())
+                atomicMin(best, (static_cast<unsigned long long>(blockIdx.y) << 40) | (off + i));
+        }
+        off += seg;
+    }
+}
+
+}  // namespace
+
+template <class T>
+int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
+             uint32_t* cavity, pma_cavity* cav, int cav_cap) {
+    check_dims(d);
+    PMA_REQUIRE(solid && dist && cavity, PMA_ERR_ARGUMENT, "pma_geodesic: null device pointer");
+    cudaStream_t s = ctx->stream;
+    const size_t n = voxels(d);
+    const Geo g{d.sx, d.sy, d.sz};
+    const int d3q7 = st == PMA_D3Q7 ? 1 : 0;
+    const T w1 = std::sqrt(static_cast<T>(1)), w2 = std::sqrt(static_cast<T>(2)),
+            w3 = std::sqrt(static_cast<T>(3));  // SPC.cpp:31-36
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>(div_up(n, 256), ctx->num_sms * 16ull));
+
+    const uint32_t cap = static_cast<uint32_t>(std::min<size_t>(n, size_t(1) << 28));
+    int* mark = static_cast<int*>(ctx->scratch("geo.mark", n * 4));
+    auto* lists = static_cast<uint32_t*>(ctx->scratch("geo.lists", 4ull * cap * 4));
+    auto* misc = static_cast<unsigned long long*>(ctx->scratch("geo.misc", 64));
+    Frontier f;
+    for (int i = 0; i < 4; ++i) f.list[i] = lists + static_cast<size_t>(i) * cap;
+    f.count = reinterpret_cast<unsigned int*>(misc);          // 4 x u32 = misc[0..1]
+    f.overflow = reinterpret_cast<unsigned int*>(misc + 2);   // misc[2] low
+    f.walls = reinterpret_cast<unsigned int*>(misc + 3);      // misc[3] low
+    f.settled = misc + 4;
+    unsigned long long* best = misc + 5;
+    f.cap = cap;
+
+    geo_init<T><<<grid, 256, 0, s>>>(solid, n, dist, cavity, mark);
+    ctx->check_launch("geo_init");
+
+    // SPC.cpp:443-458: centre = round(size * 0.5) clipped to size - 1.
+    int sz3[3] = {d.sx, d.sy, d.sz}, c[3];
+    for (int i = 0; i < 3; ++i) c[i] = std::min(static_cast<int>(sz3[i] * 0.5 + 0.5), sz3[i] - 1);
+    int maxh = 0;
+    for (int i = 0; i < 3; ++i) maxh = std::max(maxh, std::max(sz3[i] - 1 - c[i], c[i]));
+    int walls_total = 0;
+    for (int i = 0; i < 3; ++i) walls_total += (sz3[i] == 1) ? 1 : 2;
+    const size_t center_idx = (static_cast<size_t>(c[2]) * d.sx + c[0]) * d.sy + c[1];
+
+    auto* h = static_cast<unsigned long long*>(ctx->host_staging(64));
+    int half = 0;
+    uint32_t cavity_id = 0;
+    int ncav = 0;
+    const int max_buckets_per_sync = 32;
+    const unsigned bucket_grid = static_cast<unsigned>(ctx->num_sms * 8);
+    while (true) {  // SPC.cpp:94-140
+        ++half;
+        // SelectStartingPosition (SPC.cpp:396-426)
+        bool found = false;
+        int start[3] = {0, 0, 0};
+        {
+            uint8_t sv = 1;
+            T dv = 0;
+            PMA_CUDA(cudaMemcpyAsync(&sv, solid + center_idx, 1, cudaMemcpyDeviceToHost, s));
+            PMA_CUDA(cudaMemcpyAsync(&dv, dist + center_idx, sizeof(T), cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            if (sv == 0 && dv == Bits<T>::unknown()) {
+                found = true;
+                for (int i = 0; i < 3; ++i) start[i] = c[i];
+            }
+        }
+        while (!found && half < maxh) {
+            const int nh = std::min(16, maxh - half);
+            PMA_CUDA(cudaMemsetAsync(best, 0xFF, 8, s));
+            unsigned long long face = 2ull * std::max(d.sx, std::max(d.sy, d.sz)) *
+                                      std::max(d.sx, std::max(d.sy, d.sz));
+            unsigned gx = static_cast<unsigned>(std::min<unsigned long long>((face + 255) / 256, 4096));
+            geo_shell_search<T><<<dim3(gx, nh), 256, 0, s>>>(solid, dist, g, c[0], c[1], c[2], half, nh, best);
+            ctx->check_launch("geo_shell_search");
+            PMA_CUDA(cudaMemcpyAsync(h, best, 8, cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            const unsigned long long b = h[0];
+            if (b == ~0ull) {
+                half += nh;
+                continue;
+            }
+            half += static_cast<int>(b >> 40);
+            unsigned long long flat = b & ((1ull << 40) - 1);
+            // decode in the same segment order as the kernel
+            for (int k = 0; k < 3 && !found; ++k) {
+                const int a = (k == 0) ? 1 : 0, bb = (k == 2) ? 1 : 2;
+                const int a0 = std::max(c[a] - half, 0), a1 = std::min(c[a] + half, sz3[a] - 1);
+                const int b0 = std::max(c[bb] - half, 0), b1 = std::min(c[bb] + half, sz3[bb] - 1);
+                const int f0 = std::max(c[k] - half, 0), f1 = std::min(c[k] + half, sz3[k] - 1);
+                const int nf = (f0 == f1) ? 1 : 2;
+                const unsigned long long na = a1 - a0 + 1, nb = b1 - b0 + 1, seg = nf * na * nb;
+                if (flat < seg) {
+                    const int fi = static_cast<int>(flat / (na * nb));
+                    const unsigned long long r = flat % (na * nb);
+                    start[a] = a0 + static_cast<int>(r / nb);
+                    start[bb] = b0 + static_cast<int>(r % nb);
+                    start[k] = fi == 0 ? f0 : f1;
+                    found = true;
+                } else {
+                    flat -= seg;
+                }
+            }
+            PMA_REQUIRE(found, PMA_ERR_INTERNAL, "geodesic: shell search decode failed");
+        }
+        if (!found) break;
+
+        cavity_id += 127;
+        PMA_CUDA(cudaMemsetAsync(misc, 0, 5 * 8, s));  // counts, overflow, walls, settled
+        const size_t sidx = (static_cast<size_t>(start[2]) * d.sx + start[0]) * d.sy + start[1];
+        geo_start<T><<<1, 1, 0, s>>>(f, mark, dist, static_cast<uint32_t>(sidx));
+        ctx->check_launch("geo_start");
+        int k = 0;
+        while (true) {
+            for (int i = 0; i < max_buckets_per_sync; ++i, ++k) {
+                geo_bucket<T><<<bucket_grid, 256, 0, s>>>(solid, g, d3q7, w1, w2, w3, dist, cavity,
+                                                         mark, f, k, cavity_id);
+            }
+            ctx->count_launch(max_buckets_per_sync - 1);
+            ctx->check_launch("geo_bucket");
+            PMA_CUDA(cudaMemcpyAsync(h, misc, 3 * 8, cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            const unsigned* cnt = reinterpret_cast<const unsigned*>(h);
+            PMA_REQUIRE(reinterpret_cast<const unsigned*>(h)[4] == 0, PMA_ERR_LIMIT,
+                        "geodesic: frontier list overflow");
+            // after bucket k-1: lists of buckets k and k+1 hold all pending work
+            if (cnt[k & 3] == 0 && cnt[(k + 1) & 3] == 0) break;
+        }
+        PMA_CUDA(cudaMemcpyAsync(h, misc, 5 * 8, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        const unsigned walls_bits = static_cast<unsigned>(h[3]);
+        const unsigned long long settled = h[4];
+        const int reached = __builtin_popcount(walls_bits);
+        if (ncav < cav_cap && cav) {  // SPC.cpp:143-164
+            pma_cavity& o = cav[ncav];
+            std::memset(&o, 0, sizeof(o));
+            o.id = cavity_id;
+            o.seed_x = start[0];
+            o.seed_y = start[1];
+            o.seed_z = start[2];
+            o.reached_walls = reached;
+            o.reaches_all_walls = reached == walls_total ? 1 : 0;
+            o.void_count = settled;
+            const int dx = start[0] - c[0], dy = start[1] - c[1], dz = start[2] - c[2];
+            o.distance_to_center = static_cast<float>(std::sqrt(static_cast<double>(dx * dx + dy * dy + dz * dz)));
+        }
+        ++ncav;
+        if (reached == walls_total) break;
+    }
+    return std::min(ncav, cav_cap);
+}
+
+template int geodesic<float>(pma_ctx*, const uint8_t*, pma_dims, pma_stencil, float*, uint32_t*,
+                             pma_cavity*, int);
+template int geodesic<double>(pma_ctx*, const uint8_t*, pma_dims, pma_stencil, double*, uint32_t*,
+                              pma_cavity*, int);
+
+}  // namespace pma

@@ -1,0 +1,116 @@
+// Internal runtime of the pma library: context, errors, scratch cache, launch accounting.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pma.h"
+
+namespace pma {
+
+// Error carried through the C++ layer and turned into a pma_status at the C boundary.
+struct Error : std::runtime_error {
+    pma_status status;
+    Error(pma_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+void set_last_error(const std::string& msg);
+
+#define PMA_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            throw ::pma::Error(PMA_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define PMA_REQUIRE(cond, status, msg)                                                      \
+    do {                                                                                    \
+        if (!(cond)) throw ::pma::Error(status, msg);                                       \
+    } while (0)
+
+// Runs a C++ body and maps exceptions onto the C ABI status codes.
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return PMA_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return PMA_ERR_MEMORY;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return PMA_ERR_IO;
+    } catch (...) {
+        set_last_error("unknown error");
+        return PMA_ERR_INTERNAL;
+    }
+}
+
+}  // namespace pma
+
+// Device buffers cached by name; grow-only until trimmed.
+struct pma_ctx {
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::atomic<uint64_t> launches{0};
+    struct Buf {
+        void* ptr = nullptr;
+        size_t bytes = 0;
+    };
+    std::map<std::string, Buf> cache;
+    void* pinned = nullptr;       // small pinned host staging area
+    size_t pinned_bytes = 0;
+
+    void* scratch(const std::string& tag, size_t bytes);
+    void* host_staging(size_t bytes);
+    void sync();
+    void check_launch(const char* what);
+    void count_launch(uint64_t n = 1) { launches.fetch_add(n, std::memory_order_relaxed); }
+};
+
+struct pma_table {
+    std::vector<pma_pore> pores;
+    std::vector<pma_throat> throats;
+    std::vector<uint32_t> pool;
+};
+
+namespace pma {
+
+inline unsigned div_up(size_t a, size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
+
+inline void check_dims(pma_dims d) {
+    PMA_REQUIRE(d.sx > 0 && d.sy > 0 && d.sz > 0, PMA_ERR_ARGUMENT, "volume dimensions must be positive");
+    unsigned long long n = 1ull * d.sx * d.sy * d.sz;
+    PMA_REQUIRE(n < (1ull << 32), PMA_ERR_ARGUMENT, "volume must hold fewer than 2^32 voxels");
+}
+
+inline size_t voxels(pma_dims d) { return static_cast<size_t>(d.sx) * d.sy * d.sz; }
+
+// Stage implementations (device pointers, ctx stream).
+void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats* stats,
+         uint64_t* h_hist, size_t hist_cap);
+void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t max_edt2,
+                      uint32_t* crad2, uint32_t* cx, uint32_t* cy, uint32_t* cz, uint8_t* mask,
+                      uint64_t* count);
+template <class T>
+int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
+             uint32_t* cavity, pma_cavity* cav, int cav_cap);
+pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const uint32_t* crad2,
+                 pma_dims d, pma_stencil st, uint32_t* labels);
+void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d);
+pma_table* watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* crad2, pma_dims d,
+                     pma_stencil st, uint32_t max_edt2, uint32_t* labels);
+
+}  // namespace pma
