@@ -1,0 +1,332 @@
+"""Benchmark of the pore-throat + geodesic pipeline on one GB300.
+
+One step = the full pipeline over one synthetic volume: EDT -> containing balls -> seeds and
+pore propagation -> empty-pore removal -> watershed, plus float64 geodesics
+(EuclideanDistanceComputer .. WatershedComputer and ShortestPathComputer of the reference).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload grf512|spinodal1024|union128]
+  python bench.py --impl reference ...   the CPU restatement (oracle) on bounded samples
+
+Prints one JSON line. `value` is Gvoxel/s with the volume resident in HBM; `e2e` is the same
+metric through pma_pipeline_host with pinned host buffers (volume in, watershed labels and
+float64 geodesics out, copies inside the timed region). The working set (GBs of fields)
+exceeds the 129 MB L2 between steps. With N > 1 (torchrun), each rank runs its own replica on
+its own GPU: the path has no exchange step, so scaling is weak and value sums the ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "grf512": dict(kind="grf", shape=(512, 512, 512), sigma=3.0, porosity=0.65, seed=2,
+                   desc="512^3 thresholded Gaussian random field, sigma 3, porosity 0.65"),
+    "spinodal1024": dict(kind="spinodal", shape=(1024, 1024, 1024), seed=3,
+                         desc="1024^3 leveled-wave spinodal, 1000 waves, wavelength 48, porosity 0.70"),
+    "union128": dict(kind="union", shape=(128, 128, 128), seed=1,
+                     desc="128^3 union of 300 spheres, radii U[5,10]"),
+}
+
+# Algorithmic HBM bytes per voxel of the timed kernels (reads + writes each kernel must do).
+ALGO_BYTES = {
+    "edt_pass_x": 5.0,          # 1 B mask read + 4 B write
+    "edt_pass_y": 8.0,          # 4 B read + 4 B write
+    "edt_pass_z": 8.0,          # 4 B read + 4 B write
+    "balls_candidates": 16.0,   # 2 x (4 B EDT read) + 8 B key init write
+    "balls_scatter": 8.0,       # each voxel's 8 B key updated at least once
+    "uf_hook": 12.0,            # 4 B crad read + 4 B parent read + 4 B parent write
+    "geo_bucket": 17.0,         # per settled voxel: 1 B mask + 8 B read + 8 B write (float64)
+    "level_sets": 0.0,          # plateau graph work, not per voxel
+    "ws_touch": 0.0,
+}
+
+
+def make_volume(name, device):
+    import torch
+    from porousmediaanalysis_gb300 import synth
+    w = WORKLOADS[name]
+    if w["kind"] == "grf":
+        return synth.grf(w["shape"], sigma=w["sigma"], porosity=w["porosity"], seed=w["seed"], device=device)
+    if w["kind"] == "spinodal":
+        return synth.spinodal(w["shape"], seed=w["seed"], device=device)
+    return torch.from_numpy(synth.sphere_union(w["shape"], seed=w["seed"])).to(device)
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in self.rows if num(r[0])]
+        mx = [num(r[1]) for r in self.rows if num(r[1])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def device_step(pma, ctx, solid):
+    edt2, mx, _ = pma.compute_euclidean_distances(ctx, solid)
+    crad2, cx, cy, cz, mask, nb = pma.set_containing_balls(ctx, edt2, mx)
+    labels, table = pma.assign_pore_and_throat_ids(ctx, mask, edt2, crad2)
+    pma.remove_empty_pores(ctx, table, labels)
+    ws, ws_table = pma.assign_watershed_ids(ctx, table, crad2, mx)
+    dist, cav, cavities = pma.compute_shortest_path_distances(ctx, solid, fp64=True)
+    return dict(max_edt2=mx, maximum_balls=nb, pores=len(table.rows()[0]),
+                ws_throats=len(ws_table.rows()[1]), cavities=len(cavities))
+
+
+def cpu_sample_volume(name):
+    """A bounded CPU sample with the workload's structure: a 48^3 block of the same generator."""
+    import numpy as np
+    from porousmediaanalysis_gb300 import synth
+    w = WORKLOADS[name]
+    if w["kind"] == "union":
+        return synth.sphere_union((64, 64, 64), count=38, seed=w["seed"])
+    if w["kind"] == "grf":
+        return synth.grf((48, 48, 48), sigma=w["sigma"], porosity=w["porosity"], seed=w["seed"])
+    import torch
+    v = synth.spinodal((48, 48, 48), seed=w["seed"], device="cuda" if torch.cuda.is_available() else "cpu")
+    return np.ascontiguousarray(v.cpu().numpy())
+
+
+def time_oracle(vol):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    t0 = time.perf_counter()
+    oracle.full(vol, geodesic_too=False)
+    oracle.geodesic(vol, fp64=True)
+    return time.perf_counter() - t0
+
+
+def _oracle_worker(args):
+    name, reps = args
+    vol = cpu_sample_volume(name)
+    n = 0
+    t = 0.0
+    for _ in range(reps):
+        t += time_oracle(vol)
+        n += vol.size
+    return n, t
+
+
+def run_reference(args, workload):
+    """CPU restatement of the reference on bounded samples, on all host cores."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    ctxm = mp.get_context("spawn")
+    with ctxm.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_oracle_worker, [(workload, 1)] * cores)
+        t0 = time.perf_counter()
+        voxels = 0
+        for _ in range(args.steps):
+            res = pool.map(_oracle_worker, [(workload, 1)] * cores)
+            voxels += sum(r[0] for r in res)
+        wall = time.perf_counter() - t0
+    value = voxels / wall / 1e9
+    line = {
+        "impl": "reference", "metric": "pipeline_throughput", "value": value, "unit": "Gvoxel/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32+f64", "data": "synthetic",
+        "config": {"workload": workload, "desc": WORKLOADS[workload]["desc"],
+                   "cpu_sample": "48^3 block of the same generator per core per step"},
+        "cpu_baseline": {"value": value, "unit": "Gvoxel/s", "cores": cores, "kind": "port",
+                         "sample": "one 48^3 block per core per step, full pipeline + float64 geodesics"},
+        "e2e": {"value": value, "unit": "Gvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="grf512", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="pma", choices=["pma", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args, args.workload)
+
+    import torch
+    import torch.distributed as dist
+    import porousmediaanalysis_gb300 as pma
+    from porousmediaanalysis_gb300 import build as pbuild
+    pbuild.build()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    solid = make_volume(args.workload, dev)
+    torch.cuda.synchronize()
+    nvox = solid.numel()
+    ctx = pma.Context(local)
+
+    for _ in range(args.warmup):
+        info = device_step(pma, ctx, solid)
+    torch.cuda.synchronize()
+
+    # Device-resident timed region (CUDA events on the context's stream).
+    ctx.set_timing(True)
+    ctx.timing_report()
+    launches0 = ctx.launch_count
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(args.steps):
+            info = device_step(pma, ctx, solid)
+        stop.record()
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches = ctx.launch_count - launches0
+    ms = start.elapsed_time(stop)
+    kern = ctx.timing_report()
+    ctx.set_timing(False)
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * nvox * args.steps / (ms_max / 1e3) / 1e9
+
+    # End-to-end through the C ABI with pinned host buffers.
+    import numpy as np
+    h_solid = solid.cpu().pin_memory()
+    h_ws = torch.empty(solid.shape, dtype=torch.int32).pin_memory()
+    h_dist = torch.empty(solid.shape, dtype=torch.float64).pin_memory()
+    outs = {"watershed_labels": h_ws.numpy().view(np.uint32), "dist_f64": h_dist.numpy()}
+    pma.pipeline_host(ctx, h_solid.numpy(), fp64=True, fields=("watershed_labels", "dist_f64"),
+                      out_arrays=outs)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pma.pipeline_host(ctx, h_solid.numpy(), fp64=True, fields=("watershed_labels", "dist_f64"),
+                          out_arrays=outs)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * nvox * args.steps / float(te.item()) / 1e9
+
+    # Roofline of the dominant timed kernel.
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    dom = max(kern.items(), key=lambda kv: kv[1][0]) if kern else ("none", (0.0, 1))
+    name, (tot_ms, nlaunch) = dom
+    per_launch_ms = tot_ms / max(nlaunch, 1)
+    units_per_launch = nvox * args.steps / max(nlaunch, 1)
+    algo = ALGO_BYTES.get(name, 0.0) * units_per_launch
+    achieved = algo / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                "kernel_ms_per_step": tot_ms / args.steps,
+                "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(kern.items())}}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        vol = cpu_sample_volume(args.workload)
+        secs = time_oracle(vol)
+        cpu = {"value": vol.size / secs / 1e9, "unit": "Gvoxel/s", "cores": 1, "kind": "port",
+               "sample": "%s block of the same generator, full pipeline + float64 geodesics" %
+                         ("x".join(map(str, vol.shape)))}
+
+    if rank == 0:
+        line = {
+            "metric": "pipeline_throughput", "value": value, "unit": "Gvoxel/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                       "voxels": nvox, "l2": "working set of several GB exceeds L2 between steps",
+                       "stages": "edt, containing balls, pores, removal, watershed, fp64 geodesics",
+                       "result": info},
+            "e2e": {"value": e2e_value, "unit": "Gvoxel/s", "h2d_bytes_per_step": nvox,
+                    "d2h_bytes_per_step": nvox * 12},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -58,6 +58,11 @@ int pma_ctx_destroy(pma_ctx* ctx);
 int pma_ctx_set_stream(pma_ctx* ctx, void* cuda_stream);
 /* Number of this library's kernels launched through ctx since creation. */
 uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
+/* Opt-in kernel timing: with timing on, the hot kernels are bracketed by CUDA events on
+ * the context's stream. The report is a JSON object {"kernel": [total_ms, launches], ...}
+ * of everything timed since the previous report; returns its full length. */
+int pma_ctx_set_timing(pma_ctx* ctx, int enable);
+size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap);
 /* Device bytes held by ctx's scratch cache; pma_ctx_trim releases them. */
 size_t pma_ctx_scratch_bytes(const pma_ctx* ctx);
 int pma_ctx_trim(pma_ctx* ctx);
@@ -120,8 +125,9 @@ void pma_table_free(pma_table* t);
  * PoreAndThroatComputer::AssignPoreAndThroatIds (PoreAndThroatComputer.cpp:35-55; seeds
  * :93-163, propagation :192-269, pixel states BasePoreAndThroatComputer.cpp:37-133).
  * Pore ids, seeds, radii, volumes, boundary flags and every voxel's pore set are exact.
- * Throat ids are numbered in a breadth-first creation order; the reference numbers them
- * in its depth-first creation order, so throat ids match it up to a one-to-one renaming.
+ * Throat ids count down from UINT32_MAX - 1 in order of (last pore of the throat, first
+ * voxel of the throat); the reference numbers them in its depth-first creation order, so
+ * throat ids match it up to a one-to-one renaming.
  * d_labels is written completely. */
 int pma_pores(pma_ctx* ctx, const uint8_t* d_maxball_mask, const uint32_t* d_edt2,
               const uint32_t* d_crad2, pma_dims dims, pma_stencil stencil, uint32_t* d_labels,
@@ -171,8 +177,8 @@ typedef struct pma_outputs {
     uint8_t* maxball_mask;      /* IsMaximumBall */
     uint32_t* pore_labels;      /* PoreThroatIds (after empty-pore removal) */
     uint32_t* watershed_labels; /* PoreThroatIdsWatershed */
-    float* dist_f32;            /* ShortestPathDistances, float32 */
-    double* dist_f64;           /* geodesics in float64 (computed only when non-NULL) */
+    float* dist_f32;            /* ShortestPathDistances, float32 (geodesic_fp64 = 0) */
+    double* dist_f64;           /* geodesics in float64 (geodesic_fp64 = 1) */
     uint32_t* cavity;           /* CavityIds */
     /* results filled by the call */
     pma_edt_stats edt_stats;
@@ -188,7 +194,7 @@ typedef struct pma_options {
     pma_stencil stencil;
     int run_pores;              /* 1: EDT..watershed */
     int run_geodesic;           /* 1: geodesics */
-    int pad_;
+    int geodesic_fp64;          /* 1: geodesics in float64 only (dist_f64), 0: float32 */
 } pma_options;
 
 int pma_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims,

@@ -64,6 +64,17 @@ class Context:
     def scratch_bytes(self):
         return capi.lib().pma_ctx_scratch_bytes(self.handle)
 
+    def set_timing(self, enable=True):
+        capi.check(capi.lib().pma_ctx_set_timing(self.handle, int(enable)))
+
+    def timing_report(self):
+        """{kernel: (total_ms, launches)} of timed kernels since the previous report."""
+        import json
+        n = capi.lib().pma_ctx_timing_report(self.handle, None, 0)
+        buf = ctypes.create_string_buffer(n + 1)
+        capi.lib().pma_ctx_timing_report(self.handle, buf, n + 1)
+        return {k: tuple(v) for k, v in json.loads(buf.value.decode()).items()}
+
 
 class Table:
     """Owning wrapper of a pma_table (pores + throats)."""
@@ -181,27 +192,27 @@ def run_folder(ctx, base_folder, mode=MODE_ALL):
 
 
 def pipeline_host(ctx, solid_np, stencil=D3Q27, run_pores=True, run_geodesic=True, fp64=False,
-                  fields=("watershed_labels", "dist_f32")):
-    """Whole pipeline on a host (SZ, SX, SY) uint8 numpy array (pinned copies inside).
-    Returns a dict of numpy outputs for `fields`, plus tables and statistics."""
+                  fields=("watershed_labels", "dist_f32"), out_arrays=None):
+    """Whole pipeline on a host (SZ, SX, SY) uint8 array through pma_pipeline_host (the
+    host<->device copies happen inside the call). Returns a dict of numpy outputs for
+    `fields` (geodesics in float64 with fp64=True: field "dist_f64"), plus tables and
+    statistics. out_arrays may supply preallocated (e.g. pinned) numpy outputs."""
     import numpy as np
     solid_np = np.ascontiguousarray(solid_np, dtype=np.uint8)
     out = capi.Outputs()
-    res = {}
+    res = dict(out_arrays or {})
     kinds = {"edt2": np.uint32, "crad2": np.uint32, "cx": np.uint32, "cy": np.uint32,
              "cz": np.uint32, "maxball_mask": np.uint8, "pore_labels": np.uint32,
              "watershed_labels": np.uint32, "dist_f32": np.float32, "dist_f64": np.float64,
              "cavity": np.uint32}
     for name in fields:
-        arr = np.empty(solid_np.shape, dtype=kinds[name])
-        res[name] = arr
+        arr = res.get(name)
+        if arr is None:
+            arr = np.empty(solid_np.shape, dtype=kinds[name])
+            res[name] = arr
         ctype = type(getattr(out, name))
         setattr(out, name, ctypes.cast(arr.ctypes.data, ctype))
-    if fp64 and "dist_f64" not in res:
-        arr = np.empty(solid_np.shape, dtype=np.float64)
-        res["dist_f64"] = arr
-        out.dist_f64 = ctypes.cast(arr.ctypes.data, ctypes.POINTER(ctypes.c_double))
-    opts = capi.Options(stencil, int(run_pores), int(run_geodesic), 0)
+    opts = capi.Options(stencil, int(run_pores), int(run_geodesic), int(fp64))
     capi.check(capi.lib().pma_pipeline_host(ctx.handle, solid_np.ctypes.data, capi.Dims(
         solid_np.shape[1], solid_np.shape[2], solid_np.shape[0]), ctypes.byref(opts),
         ctypes.byref(out)))

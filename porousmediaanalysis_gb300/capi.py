@@ -61,7 +61,7 @@ class Outputs(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("stencil", ctypes.c_int), ("run_pores", ctypes.c_int),
-                ("run_geodesic", ctypes.c_int), ("pad_", ctypes.c_int)]
+                ("run_geodesic", ctypes.c_int), ("geodesic_fp64", ctypes.c_int)]
 
 
 _SIGNATURES = {
@@ -72,6 +72,8 @@ _SIGNATURES = {
     "pma_ctx_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pma_ctx_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
     "pma_ctx_scratch_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "pma_ctx_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "pma_ctx_timing_report": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "pma_ctx_trim": (ctypes.c_int, [ctypes.c_void_p]),
     "pma_edt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_void_p,
                                ctypes.POINTER(EdtStats), ctypes.c_void_p, ctypes.c_size_t]),

@@ -96,14 +96,19 @@ __device__ __forceinline__ bool dominated(const uint32_t* __restrict__ edt2, Geo
 // Pass 1 (count) and pass 2 (place) of the counting sort of surviving centres by r^2.
 template <bool kPlace>
 __global__ void balls_candidates(const uint32_t* __restrict__ edt2, Geo g, size_t n,
-                                 const uint32_t* __restrict__ mtab, uint32_t ntab,
+                                 const uint32_t* __restrict__ mtab, uint32_t ntab, uint32_t nR,
                                  uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
-                                 uint32_t* __restrict__ list, unsigned long long* __restrict__ keys) {
+                                 uint32_t* __restrict__ list, unsigned long long* __restrict__ keys,
+                                 unsigned int* __restrict__ err) {
     for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
          v += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const uint32_t R = edt2[v];
         if (!kPlace) keys[v] = (R == 0) ? ~0ull : 0ull;  // solid voxels never change
         if (R == 0) continue;
+        if (R >= nR) {  // max_edt2 below the data: refuse rather than index past counts
+            atomicOr(err, 1u);
+            continue;
+        }
         const int y = static_cast<int>(v % g.SY);
         const size_t zx = v / g.SY;
         const int x = static_cast<int>(zx % g.SX);
@@ -195,12 +200,13 @@ __global__ void balls_scatter(const uint32_t* __restrict__ edt2, Geo g,
 __global__ void balls_unpack(const unsigned long long* __restrict__ keys, Geo g, size_t n,
                              uint32_t* __restrict__ crad2, uint32_t* __restrict__ cxo,
                              uint32_t* __restrict__ cyo, uint32_t* __restrict__ czo,
-                             uint8_t* __restrict__ mask) {
+                             uint8_t* __restrict__ mask, unsigned int* __restrict__ err) {
     const uint32_t syz = static_cast<uint32_t>(g.SY) * g.SZ;
     for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
          v += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const unsigned long long k = keys[v];
-        if (k == ~0ull) {
+        if (k == 0) atomicOr(err, 2u);  // a void voxel no kept ball covers: internal error
+        if (k == ~0ull || k == 0) {
             crad2[v] = 0;
             cxo[v] = 0xFFFFFFFFu;
             cyo[v] = 0xFFFFFFFFu;
@@ -222,12 +228,14 @@ __global__ void balls_unpack(const unsigned long long* __restrict__ keys, Geo g,
 // coordinate arrays.
 __global__ void balls_mark(const unsigned long long* __restrict__ keys, Geo g, size_t n,
                            uint8_t* __restrict__ mask) {
+    const uint32_t limit = static_cast<uint32_t>(n);
     const uint32_t syz = static_cast<uint32_t>(g.SY) * g.SZ;
     for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
          v += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const unsigned long long k = keys[v];
-        if (k == ~0ull) continue;
+        if (k == ~0ull || k == 0) continue;
         const uint32_t lex = 0xFFFFFFFFu - static_cast<uint32_t>(k);
+        if (lex >= limit) continue;
         const uint32_t x = lex / syz, rem = lex % syz;
         mask[g.idx(static_cast<int>(x), static_cast<int>(rem / g.SZ), static_cast<int>(rem % g.SZ))] = 255;
     }
@@ -260,28 +268,38 @@ void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t m
 
     auto* keys = static_cast<unsigned long long*>(ctx->scratch("balls.keys", n * 8));
     auto* mtab = static_cast<uint32_t*>(ctx->scratch("balls.mtab", 3ull * ntab * 4));
-    auto* counts = static_cast<uint32_t*>(ctx->scratch("balls.counts", (2ull * nR + 4) * 4));
+    auto* counts = static_cast<uint32_t*>(ctx->scratch("balls.counts", (2ull * nR + 6) * 4));
     uint32_t* cursor = counts + nR;
-    uint32_t* misc = cursor + nR;  // [0] total, [1] next
+    uint32_t* misc = cursor + nR;  // [0] total, [1] next, [2..3] count, [4] error flags
     auto* list = static_cast<uint32_t*>(ctx->scratch("balls.list", n * 4));
 
     balls_containment_table<<<div_up(ntab, 128), 128, 0, s>>>(mtab, mtab + ntab, mtab + 2 * ntab, ntab);
     ctx->check_launch("balls_containment_table");
-    PMA_CUDA(cudaMemsetAsync(counts, 0, (2ull * nR + 4) * 4, s));
-    balls_candidates<false><<<grid, 256, 0, s>>>(edt2, g, n, mtab, ntab, counts, nullptr, nullptr, keys);
+    PMA_CUDA(cudaMemsetAsync(counts, 0, (2ull * nR + 6) * 4, s));
+    unsigned int* err = misc + 4;
+    {
+    KernelTimer kt(ctx, "balls_candidates");
+    balls_candidates<false><<<grid, 256, 0, s>>>(edt2, g, n, mtab, ntab, nR, counts, nullptr, nullptr,
+                                                 keys, err);
     ctx->check_launch("balls_candidates(count)");
     balls_bucket_offsets<<<1, 1024, 0, s>>>(counts, cursor, nR, misc);
     ctx->check_launch("balls_bucket_offsets");
-    balls_candidates<true><<<grid, 256, 0, s>>>(edt2, g, n, mtab, ntab, counts, cursor, list, keys);
+    balls_candidates<true><<<grid, 256, 0, s>>>(edt2, g, n, mtab, ntab, nR, counts, cursor, list,
+                                                keys, err);
     ctx->check_launch("balls_candidates(place)");
-    uint32_t total = 0;
-    PMA_CUDA(cudaMemcpyAsync(&total, misc, 4, cudaMemcpyDeviceToHost, s));
+    }
+    uint32_t hm[5] = {0, 0, 0, 0, 0};
+    PMA_CUDA(cudaMemcpyAsync(hm, misc, sizeof(hm), cudaMemcpyDeviceToHost, s));
     ctx->sync();
+    PMA_REQUIRE(!(hm[4] & 1u), PMA_ERR_ARGUMENT,
+                "pma_containing_balls: max_edt2 is smaller than the largest squared distance");
+    const uint32_t total = hm[0];
     if (total) {
+        KernelTimer kt(ctx, "balls_scatter");
         balls_scatter<<<ctx->num_sms * 8, 256, 0, s>>>(edt2, g, list, total, misc + 1, keys);
         ctx->check_launch("balls_scatter");
     }
-    balls_unpack<<<grid, 256, 0, s>>>(keys, g, n, crad2, cx, cy, cz, mask);
+    balls_unpack<<<grid, 256, 0, s>>>(keys, g, n, crad2, cx, cy, cz, mask, err);
     ctx->check_launch("balls_unpack");
     balls_mark<<<grid, 256, 0, s>>>(keys, g, n, mask);
     ctx->check_launch("balls_mark");
@@ -291,7 +309,9 @@ void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t m
     ctx->check_launch("count_value");
     unsigned long long c = 0;
     PMA_CUDA(cudaMemcpyAsync(&c, d_count, 8, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(hm, misc, sizeof(hm), cudaMemcpyDeviceToHost, s));
     ctx->sync();
+    PMA_REQUIRE(!(hm[4] & 2u), PMA_ERR_INTERNAL, "pma_containing_balls: uncovered void voxel");
     if (count) *count = c;
 }
 

@@ -1,6 +1,8 @@
 // C ABI of the pma library (include/pma.h): context, errors, tables and stage wrappers.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 
 #include "pma_internal.h"
@@ -123,6 +125,47 @@ int pma_ctx_set_stream(pma_ctx* ctx, void* stream) {
 }
 
 uint64_t pma_ctx_launch_count(const pma_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
+
+int pma_ctx_set_timing(pma_ctx* ctx, int enable) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        ctx->timing = enable != 0;
+    });
+}
+
+size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap) {
+    std::string out = "{";
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        std::map<std::string, std::pair<double, long long>> acc;
+        for (auto& t : ctx->timed) {
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, t.start, t.stop) == cudaSuccess) {
+                acc[t.name].first += ms;
+                acc[t.name].second += 1;
+            }
+            cudaEventDestroy(t.start);
+            cudaEventDestroy(t.stop);
+        }
+        ctx->timed.clear();
+        bool first = true;
+        char item[256];
+        for (auto& kv : acc) {
+            std::snprintf(item, sizeof(item), "%s\"%s\": [%.6f, %lld]", first ? "" : ", ", kv.first.c_str(),
+                          kv.second.first, kv.second.second);
+            out += item;
+            first = false;
+        }
+    }
+    out += "}";
+    if (buf && cap) {
+        size_t n = std::min(cap - 1, out.size());
+        std::memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    }
+    return out.size();
+}
 
 size_t pma_ctx_scratch_bytes(const pma_ctx* ctx) {
     size_t s = 0;

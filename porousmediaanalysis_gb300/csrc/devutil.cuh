@@ -1,0 +1,124 @@
+// Device helpers shared by the pore and watershed stages: volume geometry, the reference's
+// neighbour order and thin wrappers over CUB's order-preserving select, scan and sort.
+#pragma once
+
+#include <cub/cub.cuh>
+
+#include "pma_internal.h"
+
+namespace pma {
+
+struct Grid {
+    int SX, SY, SZ;
+    __host__ __device__ __forceinline__ size_t idx(int x, int y, int z) const {
+        return (static_cast<size_t>(z) * SX + x) * SY + y;
+    }
+    __host__ __device__ __forceinline__ void coords(size_t v, int& x, int& y, int& z) const {
+        y = static_cast<int>(v % SY);
+        const size_t zx = v / SY;
+        x = static_cast<int>(zx % SX);
+        z = static_cast<int>(zx / SX);
+    }
+    __host__ __device__ __forceinline__ bool inside(int x, int y, int z) const {
+        return x >= 0 && x < SX && y >= 0 && y < SY && z >= 0 && z < SZ;
+    }
+    __host__ __device__ __forceinline__ bool on_face(int x, int y, int z) const {
+        return x == 0 || y == 0 || z == 0 || x == SX - 1 || y == SY - 1 || z == SZ - 1;
+    }
+};
+
+// Neighbour j in 0..26 in the reference's loop order (x outer, then y, then z, each -1..1;
+// e.g. PoreAndThroatComputer.cpp:228-234). Returns false for the centre and, with D3Q7,
+// for diagonal offsets (ModelUtilities.h:295-302).
+__device__ __forceinline__ bool stencil_offset(int j, bool d3q7, int& dx, int& dy, int& dz) {
+    dx = j / 9 - 1;
+    dy = (j / 3) % 3 - 1;
+    dz = j % 3 - 1;
+    if (j == 13) return false;
+    if (d3q7 && (dx != 0) + (dy != 0) + (dz != 0) > 1) return false;
+    return true;
+}
+
+// --- CUB wrappers (all on ctx->stream; temporary storage cached in the context) ----------
+
+template <class InIt, class T>
+inline int64_t select_flagged(pma_ctx* ctx, InIt in, const uint8_t* flags, T* out, int64_t n,
+                              int64_t* d_count) {
+    size_t bytes = 0;
+    PMA_CUDA(cub::DeviceSelect::Flagged(nullptr, bytes, in, flags, out, d_count, n, ctx->stream));
+    void* tmp = ctx->scratch("cub.tmp", bytes);
+    PMA_CUDA(cub::DeviceSelect::Flagged(tmp, bytes, in, flags, out, d_count, n, ctx->stream));
+    int64_t h = 0;
+    PMA_CUDA(cudaMemcpyAsync(&h, d_count, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    ctx->count_launch(1);
+    return h;
+}
+
+template <class T>
+inline void exclusive_sum(pma_ctx* ctx, const T* in, T* out, int64_t n) {
+    size_t bytes = 0;
+    PMA_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, ctx->stream));
+    void* tmp = ctx->scratch("cub.tmp", bytes);
+    PMA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, n, ctx->stream));
+    ctx->count_launch(1);
+}
+
+template <class K, class V>
+inline void sort_pairs(pma_ctx* ctx, const K* kin, K* kout, const V* vin, V* vout, int64_t n,
+                       int end_bit = sizeof(K) * 8) {
+    size_t bytes = 0;
+    PMA_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, bytes, kin, kout, vin, vout, n, 0, end_bit,
+                                             ctx->stream));
+    void* tmp = ctx->scratch("cub.tmp", bytes);
+    PMA_CUDA(cub::DeviceRadixSort::SortPairs(tmp, bytes, kin, kout, vin, vout, n, 0, end_bit,
+                                             ctx->stream));
+    ctx->count_launch(1);
+}
+
+template <class K>
+inline void sort_keys(pma_ctx* ctx, const K* kin, K* kout, int64_t n, int end_bit = sizeof(K) * 8) {
+    size_t bytes = 0;
+    PMA_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, bytes, kin, kout, n, 0, end_bit, ctx->stream));
+    void* tmp = ctx->scratch("cub.tmp", bytes);
+    PMA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, bytes, kin, kout, n, 0, end_bit, ctx->stream));
+    ctx->count_launch(1);
+}
+
+template <class T>
+inline int64_t unique(pma_ctx* ctx, const T* in, T* out, int64_t n, int64_t* d_count) {
+    size_t bytes = 0;
+    PMA_CUDA(cub::DeviceSelect::Unique(nullptr, bytes, in, out, d_count, n, ctx->stream));
+    void* tmp = ctx->scratch("cub.tmp", bytes);
+    PMA_CUDA(cub::DeviceSelect::Unique(tmp, bytes, in, out, d_count, n, ctx->stream));
+    int64_t h = 0;
+    PMA_CUDA(cudaMemcpyAsync(&h, d_count, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    ctx->count_launch(1);
+    return h;
+}
+
+inline unsigned grid_for(pma_ctx* ctx, size_t n, int threads = 256) {
+    size_t b = (n + threads - 1) / threads;
+    size_t cap = static_cast<size_t>(ctx->num_sms) * 32;
+    if (b > cap) b = cap;
+    return static_cast<unsigned>(b < 1 ? 1 : b);
+}
+
+#define PMA_GRID_STRIDE(i, n)                                                             \
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < (n); \
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+
+// Pore-id sequence of the reference: 127, 128, ... skipping past multiples of 255
+// (PoreAndThroatComputer.cpp:60, 149-153).
+inline std::vector<uint32_t> pore_id_sequence(size_t n) {
+    std::vector<uint32_t> ids(n);
+    uint32_t id = 127;
+    for (size_t i = 0; i < n; ++i) {
+        ids[i] = id;
+        id += (id % 255 == 0) ? 127 : 1;
+    }
+    return ids;
+}
+
+}  // namespace pma

@@ -199,6 +199,7 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
         PMA_CUDA(cudaFuncSetAttribute(edt_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smem)));
         const size_t cols = static_cast<size_t>(SY) * SZ;
+        KernelTimer kt(ctx, "edt_pass_x");
         edt_pass_x<<<div_up(cols, threads), threads, smem, s>>>(solid, edt2, SX, SY, SZ, words);
         ctx->check_launch("edt_pass_x");
     }
@@ -212,6 +213,7 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
                                       static_cast<int>(smem)));
         const size_t rows = static_cast<size_t>(SX) * SZ;
         size_t blocks = std::min<size_t>((rows + warps - 1) / warps, static_cast<size_t>(ctx->num_sms) * 64);
+        KernelTimer kt(ctx, "edt_pass_y");
         edt_pass_y<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(edt2, SY, rows);
         ctx->check_launch("edt_pass_y");
     }
@@ -228,6 +230,7 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
         PMA_CUDA(cudaFuncSetAttribute(edt_pass_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smem)));
         const size_t tiles = static_cast<size_t>(SX) * ((SY + kTileY - 1) / kTileY);
+        KernelTimer kt(ctx, "edt_pass_z");
         edt_pass_z<<<static_cast<unsigned>(tiles), 256, smem, s>>>(edt2, SX, SY, SZ, d_hist,
                                                                   hist_len, d_max);
         ctx->check_launch("edt_pass_z");

@@ -11,7 +11,8 @@
 // round-to-nearest fl(d + w) >= floor(d) + 1, so relaxing a voxel of bucket floor(d) = k
 // only reaches buckets k+1 and k+2. Bucket k is therefore final when it is processed and
 // one parallel sweep per bucket suffices (Dial's algorithm). Buckets live in a ring of
-// four voxel lists; a per-voxel mark keeps a voxel at most once in each bucket list.
+// four voxel lists; a per-voxel mark (the lowest bucket appended to) keeps a voxel at most
+// once in each bucket list.
 #include "pma_internal.h"
 
 #include <cfloat>
@@ -63,14 +64,16 @@ __global__ void geo_init(const uint8_t* __restrict__ solid, size_t n, T* __restr
         const bool s = solid[v] != 0;  // SPC.cpp:354-372
         dist[v] = s ? static_cast<T>(-1) : Bits<T>::unknown();
         cavity[v] = s ? 0u : 0xFFFFFFFFu;
-        mark[v] = -1;
+        mark[v] = 0x7FFFFFFF;
     }
 }
 
 template <class T>
 __device__ __forceinline__ void enqueue(const Frontier& f, int* mark, uint32_t v, T d) {
+    // A voxel's bucket only decreases; the mark keeps the lowest bucket it was appended to,
+    // so each bucket list holds a voxel at most once even when improvements race.
     const int b = Bits<T>::bucket(d);
-    if (atomicExch(&mark[v], b) == b) return;
+    if (atomicMin(&mark[v], b) <= b) return;
     const unsigned pos = atomicAdd(&f.count[b & 3], 1u);
     if (pos < f.cap) f.list[b & 3][pos] = v;
     else atomicExch(f.overflow, 1u);
@@ -289,6 +292,7 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
         ctx->check_launch("geo_start");
         int k = 0;
         while (true) {
+            KernelTimer kt(ctx, "geo_bucket");
             for (int i = 0; i < max_buckets_per_sync; ++i, ++k) {
                 geo_bucket<T><<<bucket_grid, 256, 0, s>>>(solid, g, d3q7, w1, w2, w3, dist, cavity,
                                                          mark, f, k, cavity_id);
@@ -302,6 +306,9 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
                         "geodesic: frontier list overflow");
             // after bucket k-1: lists of buckets k and k+1 hold all pending work
             if (cnt[k & 3] == 0 && cnt[(k + 1) & 3] == 0) break;
+            // Distances are below 2 per voxel step, so no bucket index can exceed 2n.
+            PMA_REQUIRE(static_cast<size_t>(k) <= 2 * n + 64, PMA_ERR_LIMIT,
+                        "geodesic: bucket sweep did not terminate");
         }
         PMA_CUDA(cudaMemcpyAsync(h, misc, 5 * 8, cudaMemcpyDeviceToHost, s));
         ctx->sync();

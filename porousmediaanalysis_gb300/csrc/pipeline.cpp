@@ -68,8 +68,9 @@ extern "C" int pma_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims 
         pma_options o{PMA_D3Q27, 1, 1, 0};
         if (opts) o = *opts;
         const size_t n = pma::voxels(dims);
-        const bool geo64 = o.run_geodesic && out->dist_f64;
-        pma::Fields f = pma::alloc_fields(ctx, n, o.run_pores != 0, o.run_geodesic != 0, geo64);
+        const bool geo64 = o.run_geodesic && o.geodesic_fp64;
+        pma::Fields f = pma::alloc_fields(ctx, n, o.run_pores != 0, o.run_geodesic != 0 && !geo64, geo64);
+        if (geo64) f.cavity = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
         PMA_CUDA(cudaMemcpyAsync(f.solid, h_solid, n, cudaMemcpyHostToDevice, ctx->stream));
         out->pores = nullptr;
         out->watershed = nullptr;
@@ -91,17 +92,16 @@ extern "C" int pma_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims 
             pma::d2h(ctx, out->pore_labels, f.labels, n);
             pma::d2h(ctx, out->watershed_labels, f.labels_ws, n);
         }
-        if (o.run_geodesic) {
+        if (o.run_geodesic && !geo64) {
             out->n_cavities = pma::geodesic<float>(ctx, f.solid, dims, o.stencil, f.dist32, f.cavity,
                                                    out->cavities, 16);
             pma::d2h(ctx, out->dist_f32, f.dist32, n);
             pma::d2h(ctx, out->cavity, f.cavity, n);
-            if (geo64) {
-                uint32_t* cav64 = static_cast<uint32_t*>(ctx->scratch("pipe.cavity64", n * 4));
-                pma_cavity tmp[16];
-                pma::geodesic<double>(ctx, f.solid, dims, o.stencil, f.dist64, cav64, tmp, 16);
-                pma::d2h(ctx, out->dist_f64, f.dist64, n);
-            }
+        } else if (o.run_geodesic) {
+            out->n_cavities = pma::geodesic<double>(ctx, f.solid, dims, o.stencil, f.dist64, f.cavity,
+                                                    out->cavities, 16);
+            pma::d2h(ctx, out->dist_f64, f.dist64, n);
+            pma::d2h(ctx, out->cavity, f.cavity, n);
         }
         ctx->sync();
     });

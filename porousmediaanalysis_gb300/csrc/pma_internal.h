@@ -72,6 +72,12 @@ struct pma_ctx {
     std::map<std::string, Buf> cache;
     void* pinned = nullptr;       // small pinned host staging area
     size_t pinned_bytes = 0;
+    bool timing = false;          // bracket hot kernels with events
+    struct Timed {
+        std::string name;
+        cudaEvent_t start, stop;
+    };
+    std::vector<Timed> timed;
 
     void* scratch(const std::string& tag, size_t bytes);
     void* host_staging(size_t bytes);
@@ -87,6 +93,23 @@ struct pma_table {
 };
 
 namespace pma {
+
+// Brackets the launches of its scope with CUDA events when the context's timing is on.
+struct KernelTimer {
+    pma_ctx* ctx;
+    const char* name;
+    cudaEvent_t start = nullptr;
+    KernelTimer(pma_ctx* c, const char* n) : ctx(c), name(n) {
+        if (ctx->timing && cudaEventCreate(&start) == cudaSuccess) cudaEventRecord(start, ctx->stream);
+    }
+    ~KernelTimer() {
+        if (!start) return;
+        cudaEvent_t stop;
+        if (cudaEventCreate(&stop) != cudaSuccess) return;
+        cudaEventRecord(stop, ctx->stream);
+        ctx->timed.push_back(pma_ctx::Timed{name, start, stop});
+    }
+};
 
 inline unsigned div_up(size_t a, size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 

@@ -1,18 +1,891 @@
-// Pore seeds, pore propagation, empty-pore removal and watershed (placeholder).
-#include "pma_internal.h"
+// Pore seeds, initial pore propagation and empty-pore removal
+// (PoreAndThroatComputer.cpp:93-269, BasePoreAndThroatComputer.cpp:37-133,
+// EmptyPoresRemover.cpp:31-244).
+//
+// The reference runs one depth-first search per pore: from the seed it follows u -> v when
+// v is a void stencil neighbour with crad(v) <= crad(u). Restated exactly:
+//  * Plateaus. Voxels of one connected set of equal crad ("plateau") all reach each other,
+//    so the set S of seeds reaching a voxel is constant on its plateau, and
+//    S(p) = union of S(q) over plateaus q with an edge into p, plus p's own seed.
+//  * Seeds. Maximum balls are visited in std::sort order and a ball starts a pore unless an
+//    earlier pore already reached its centre. By induction on that order, a ball is a seed
+//    exactly when no ball earlier in the order reaches it (a skipped ball was reached by an
+//    earlier seed, which then reaches all it reaches). With m(p) the smallest rank of a ball
+//    reaching plateau p, p's smallest-rank ball is a seed iff it beats m of every plateau
+//    with an edge into p.
+//  * Both recurrences run plateau by plateau in decreasing crad, a pair of launches per
+//    crad level. The ball order comes from std::sort on the host applied to the same
+//    sequence (z, x, y scan order) with the same comparator, so equal radii tie-break
+//    exactly as in the reference.
+//  * A voxel's label is its seed's pore id when |S| = 1 and a shared type ("throat") when
+//    |S| >= 2. Pore volumes, boundary flags, type volumes and type pore lists are exact.
+//    The reference numbers types in its depth-first creation order, which also consumed ids
+//    for types deleted later; here the surviving types are numbered by (last pore of the
+//    type, first voxel of the type), so type ids match the reference up to a one-to-one
+//    renaming.
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "devutil.cuh"
 
 namespace pma {
+namespace {
 
-pma_table* pores(pma_ctx*, const uint8_t*, const uint32_t*, const uint32_t*, pma_dims, pma_stencil,
-                 uint32_t*) {
-    throw Error(PMA_ERR_INTERNAL, "pma_pores: not available in this build");
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kUnionLimit = 1 << 22;
+
+__global__ void flag_outer(const uint8_t* __restrict__ mask, size_t n, uint8_t* __restrict__ flags) {
+    PMA_GRID_STRIDE(v, n) flags[v] = mask[v] == 255;
 }
-void remove_empty_pores(pma_ctx*, pma_table*, uint32_t*, pma_dims) {
-    throw Error(PMA_ERR_INTERNAL, "pma_remove_empty_pores: not available in this build");
+
+__global__ void gather_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
+                           size_t n, uint32_t* __restrict__ out) {
+    PMA_GRID_STRIDE(i, n) out[i] = src[idx[i]];
 }
-pma_table* watershed(pma_ctx*, const pma_table*, const uint32_t*, pma_dims, pma_stencil, uint32_t,
-                     uint32_t*) {
-    throw Error(PMA_ERR_INTERNAL, "pma_watershed: not available in this build");
+
+__global__ void fill_u32(uint32_t* __restrict__ a, size_t n, uint32_t value) {
+    PMA_GRID_STRIDE(i, n) a[i] = value;
+}
+
+__global__ void scatter_rank(const uint32_t* __restrict__ voxel_of_rank, size_t n,
+                             uint32_t* __restrict__ crank) {
+    PMA_GRID_STRIDE(r, n) crank[voxel_of_rank[r]] = static_cast<uint32_t>(r);
+}
+
+// --- union-find over equal-crad neighbours (parents always point to smaller indices) ---
+
+__device__ __forceinline__ uint32_t uf_root(uint32_t* parent, uint32_t v) {
+    uint32_t cur = parent[v];
+    if (cur == v) return v;
+    uint32_t prev = v, next;
+    while (cur > (next = parent[cur])) {
+        parent[prev] = next;  // path halving; racing writes only shorten paths
+        prev = cur;
+        cur = next;
+    }
+    return cur;
+}
+
+__global__ void uf_init(const uint32_t* __restrict__ crad, size_t n, uint32_t* __restrict__ parent) {
+    PMA_GRID_STRIDE(v, n) parent[v] = crad[v] ? static_cast<uint32_t>(v) : kNone;
+}
+
+__global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int d3q7,
+                        uint32_t* __restrict__ parent, unsigned int* __restrict__ err) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t r = crad[v];
+        if (!r) continue;
+        int x, y, z;
+        g.coords(v, x, y, z);
+        // Each unordered pair once: the 13 offsets whose linear index delta
+        // dz*SX*SY + dx*SY + dy is positive, i.e. (dz, dx, dy) > 0 lexicographically.
+        for (int k = 0; k < 13; ++k) {
+            int dx, dy, dz;
+            if (k < 4) {
+                dz = 0;
+                dx = (k == 0) ? 0 : 1;
+                dy = (k == 0) ? 1 : k - 2;
+            } else {
+                dz = 1;
+                dx = (k - 4) / 3 - 1;
+                dy = (k - 4) % 3 - 1;
+            }
+            if (d3q7 && (dx != 0) + (dy != 0) + (dz != 0) > 1) continue;
+            const int nx = x + dx, ny = y + dy, nz = z + dz;
+            if (!g.inside(nx, ny, nz)) continue;
+            const size_t w = g.idx(nx, ny, nz);
+            if (crad[w] != r) continue;
+            uint32_t a = uf_root(parent, static_cast<uint32_t>(v));
+            uint32_t b = uf_root(parent, static_cast<uint32_t>(w));
+            int it = 0;
+            while (a != b) {
+                if (++it > kUnionLimit) {
+                    atomicOr(err, 1u);
+                    break;
+                }
+                if (a < b) {
+                    const uint32_t old = atomicCAS(&parent[b], b, a);
+                    if (old == b) break;
+                    b = old;
+                } else {
+                    const uint32_t old = atomicCAS(&parent[a], a, b);
+                    if (old == a) break;
+                    a = old;
+                }
+            }
+        }
+    }
+}
+
+__global__ void uf_flatten(size_t n, uint32_t* __restrict__ parent) {
+    PMA_GRID_STRIDE(v, n) {
+        if (parent[v] != kNone) parent[v] = uf_root(parent, static_cast<uint32_t>(v));
+    }
+}
+
+__global__ void flag_roots(const uint32_t* __restrict__ parent, size_t n, uint8_t* __restrict__ flags) {
+    PMA_GRID_STRIDE(v, n) flags[v] = parent[v] == v;
+}
+
+__global__ void scatter_pid(const uint32_t* __restrict__ roots, size_t np, uint32_t* __restrict__ tmp) {
+    PMA_GRID_STRIDE(p, np) tmp[roots[p]] = static_cast<uint32_t>(p);
+}
+
+// parent[v] (the root voxel) becomes the dense plateau id.
+__global__ void to_pid(const uint32_t* __restrict__ tmp, size_t n, uint32_t* __restrict__ parent) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t r = parent[v];
+        if (r != kNone) parent[v] = tmp[r];
+    }
+}
+
+__global__ void plateau_stats(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
+                              const uint32_t* __restrict__ crank, Grid g, size_t n,
+                              uint32_t* __restrict__ pcrad, unsigned int* __restrict__ psize,
+                              unsigned int* __restrict__ pface, uint32_t* __restrict__ pminrank) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t p = pid[v];
+        if (p == kNone) continue;
+        pcrad[p] = crad[v];
+        atomicAdd(&psize[p], 1u);
+        int x, y, z;
+        g.coords(v, x, y, z);
+        if (g.on_face(x, y, z)) pface[p] = 1;
+        const uint32_t rk = crank[v];
+        if (rk != kNone) atomicMin(&pminrank[p], rk);
+    }
+}
+
+// Plateau edges q -> p (crad strictly decreasing), deduplicated per voxel.
+template <bool kWrite>
+__global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
+                              Grid g, size_t n, int d3q7, unsigned long long* __restrict__ count,
+                              unsigned long long* __restrict__ edges, unsigned long long cap) {
+    unsigned long long local = 0;
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t p = pid[v];
+        if (p == kNone) continue;
+        const uint32_t r = crad[v];
+        int x, y, z;
+        g.coords(v, x, y, z);
+        uint32_t seen[26];
+        int ns = 0;
+        for (int j = 0; j < 27; ++j) {
+            int dx, dy, dz;
+            if (!stencil_offset(j, d3q7, dx, dy, dz)) continue;
+            const int nx = x + dx, ny = y + dy, nz = z + dz;
+            if (!g.inside(nx, ny, nz)) continue;
+            const size_t w = g.idx(nx, ny, nz);
+            const uint32_t rw = crad[w];
+            if (rw == 0 || rw >= r) continue;
+            const uint32_t q = pid[w];
+            bool dup = false;
+            for (int i = 0; i < ns; ++i) dup |= seen[i] == q;
+            if (dup) continue;
+            seen[ns++] = q;
+            if (kWrite) {
+                const unsigned long long pos = atomicAdd(count, 1ull);
+                if (pos < cap) edges[pos] = (static_cast<unsigned long long>(q) << 32) | p;
+            } else {
+                ++local;
+            }
+        }
+    }
+    if (!kWrite) {
+        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
+        if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+    }
+}
+
+// CSR offsets of edges sorted by destination (key high word).
+__global__ void edge_offsets(const unsigned long long* __restrict__ edges, size_t ne, size_t np,
+                             unsigned int* __restrict__ eoff) {
+    PMA_GRID_STRIDE(i, ne + 1) {
+        const uint32_t cur = (i < ne) ? static_cast<uint32_t>(edges[i] >> 32) : static_cast<uint32_t>(np);
+        const uint32_t prev = (i == 0) ? 0u : static_cast<uint32_t>(edges[i - 1] >> 32) + 1u;
+        for (uint32_t p = prev; p <= cur && p <= np; ++p) eoff[p] = static_cast<unsigned int>(i);
+    }
+}
+
+__global__ void level_keys(const uint32_t* __restrict__ pcrad, size_t np, uint32_t* __restrict__ key,
+                           uint32_t* __restrict__ val) {
+    PMA_GRID_STRIDE(p, np) {
+        key[p] = 0xFFFFFFFFu - pcrad[p];  // ascending key = descending crad
+        val[p] = static_cast<uint32_t>(p);
+    }
+}
+
+struct PlateauSets {
+    const unsigned int* eoff;
+    const unsigned long long* edges;  // sorted by destination; low word = source
+    const uint32_t* minrank;
+    uint32_t* m;       // smallest ball rank reaching the plateau
+    uint32_t* seed;    // rank of the plateau's seed or kNone
+    unsigned long long* soff;
+    uint32_t* slen;
+    uint32_t* pool;
+    unsigned long long pool_cap;
+    unsigned int* err;
+};
+
+// First element of sorted a[0..n) greater than `last` (kNone if none).
+__device__ __forceinline__ uint32_t next_above(const uint32_t* a, uint32_t n, long long last) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (static_cast<long long>(a[mid]) > last) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo < n ? a[lo] : kNone;
+}
+
+// One plateau of the current level. kWrite = false: seeds, m and |S|; true: write S.
+template <bool kWrite>
+__global__ void level_sets(PlateauSets st, const uint32_t* __restrict__ order, size_t begin,
+                           size_t end, unsigned long long* __restrict__ cnt,
+                           const unsigned long long* __restrict__ off,
+                           const unsigned long long* __restrict__ base) {
+    for (size_t i = begin + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < end;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const uint32_t p = order[i];
+        const unsigned int e0 = st.eoff[p], e1 = st.eoff[p + 1];
+        uint32_t seed = kNone;
+        if (!kWrite) {
+            uint32_t mp = kNone;
+            for (unsigned int e = e0; e < e1; ++e) {
+                const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+                mp = min(mp, st.m[q]);
+            }
+            const uint32_t own = st.minrank[p];
+            if (own < mp) seed = own;
+            st.m[p] = min(own, mp);
+            st.seed[p] = seed;
+        } else {
+            seed = st.seed[p];
+        }
+        long long last = -1;
+        unsigned long long k = 0;
+        unsigned long long pos = kWrite ? (*base + off[i - begin]) : 0;
+        while (true) {
+            uint32_t best = (seed != kNone && static_cast<long long>(seed) > last) ? seed : kNone;
+            for (unsigned int e = e0; e < e1; ++e) {
+                const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+                const uint32_t c = next_above(st.pool + st.soff[q], st.slen[q], last);
+                best = min(best, c);
+            }
+            if (best == kNone) break;
+            if (kWrite) {
+                if (pos + k < st.pool_cap) st.pool[pos + k] = best;
+                else atomicOr(st.err, 2u);
+            }
+            ++k;
+            last = best;
+        }
+        if (kWrite) {
+            st.soff[p] = pos;
+            st.slen[p] = static_cast<uint32_t>(k);
+        } else {
+            cnt[i - begin] = k;
+        }
+    }
+}
+
+__global__ void level_advance(unsigned long long* __restrict__ base, const unsigned long long* __restrict__ off,
+                              const unsigned long long* __restrict__ cnt, size_t nlev) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *base += off[nlev - 1] + cnt[nlev - 1];
+}
+
+// FNV-1a style 64-bit hashes of a sorted rank list (two independent streams).
+__device__ __forceinline__ void list_hash(const uint32_t* a, uint32_t n, unsigned long long& h1,
+                                          unsigned long long& h2) {
+    h1 = 1469598103934665603ull ^ n;
+    h2 = 0x9E3779B97F4A7C15ull + n;
+    for (uint32_t i = 0; i < n; ++i) {
+        h1 = (h1 ^ a[i]) * 1099511628211ull;
+        h2 = (h2 + a[i] + 0x632BE59BD9B4E019ull) * 0xD6E8FEB86659FD93ull;
+        h2 ^= h2 >> 32;
+    }
+}
+
+__global__ void throat_hashes(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
+                              const uint32_t* __restrict__ pool, const uint32_t* __restrict__ multi,
+                              size_t nm, unsigned long long* __restrict__ h1o,
+                              unsigned long long* __restrict__ h2o) {
+    PMA_GRID_STRIDE(i, nm) {
+        const uint32_t p = multi[i];
+        unsigned long long a, b;
+        list_hash(pool + soff[p], slen[p], a, b);
+        h1o[i] = a;
+        h2o[i] = b;
+    }
+}
+
+__global__ void flag_multi(const uint32_t* __restrict__ slen, size_t np, uint8_t* __restrict__ f) {
+    PMA_GRID_STRIDE(p, np) f[p] = slen[p] >= 2;
+}
+
+// Group starts among plateaus sorted by (h1, h2); verifies list equality within groups.
+__global__ void group_starts(const uint32_t* __restrict__ sorted_p, const unsigned long long* __restrict__ h1,
+                             const unsigned long long* __restrict__ h2, size_t nm,
+                             const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
+                             const uint32_t* __restrict__ pool, uint32_t* __restrict__ start,
+                             unsigned int* __restrict__ err) {
+    PMA_GRID_STRIDE(i, nm) {
+        bool s = (i == 0) || h1[i] != h1[i - 1] || h2[i] != h2[i - 1];
+        if (!s) {
+            const uint32_t a = sorted_p[i], b = sorted_p[i - 1];
+            bool eq = slen[a] == slen[b];
+            for (uint32_t k = 0; eq && k < slen[a]; ++k) eq = pool[soff[a] + k] == pool[soff[b] + k];
+            if (!eq) atomicOr(err, 4u);  // 128-bit hash collision between different sets
+        }
+        start[i] = s ? 1u : 0u;
+    }
+}
+
+struct GroupOut {
+    uint32_t* group_of;             // per multi index (sorted order) -> group
+    unsigned long long* gvol;       // per group
+    unsigned long long* gfirst;     // per group: smallest root voxel index
+    uint32_t* grep;                 // per group: representative plateau
+};
+
+__global__ void group_reduce(const uint32_t* __restrict__ sorted_p, const uint32_t* __restrict__ gid,
+                             size_t nm, const unsigned int* __restrict__ psize,
+                             const uint32_t* __restrict__ roots, GroupOut go,
+                             uint32_t* __restrict__ plateau_group) {
+    PMA_GRID_STRIDE(i, nm) {
+        const uint32_t p = sorted_p[i];
+        const uint32_t gr = gid[i];
+        plateau_group[p] = gr;
+        atomicAdd(&go.gvol[gr], static_cast<unsigned long long>(psize[p]));
+        atomicMin(&go.gfirst[gr], static_cast<unsigned long long>(roots[p]));
+        if (i == 0 || gid[i - 1] != gr) go.grep[gr] = p;
+    }
+}
+
+struct PoreAcc {
+    const uint32_t* rank2pore;       // ball rank -> pore index (kNone if not a seed)
+    unsigned long long* pvol;
+    unsigned int* pbound;
+};
+
+__global__ void pore_accumulate(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
+                                const uint32_t* __restrict__ pool, const unsigned int* __restrict__ psize,
+                                const unsigned int* __restrict__ pface, size_t np, PoreAcc pa) {
+    PMA_GRID_STRIDE(p, np) {
+        const uint32_t n = slen[p];
+        const uint32_t* s = pool + soff[p];
+        if (n == 1) atomicAdd(&pa.pvol[pa.rank2pore[s[0]]], static_cast<unsigned long long>(psize[p]));
+        if (pface[p])
+            for (uint32_t k = 0; k < n; ++k) pa.pbound[pa.rank2pore[s[k]]] = 1;
+    }
+}
+
+__global__ void plateau_labels(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
+                               const uint32_t* __restrict__ pool, const uint32_t* __restrict__ rank2id,
+                               const uint32_t* __restrict__ plateau_group,
+                               const uint32_t* __restrict__ group_tid, size_t np,
+                               uint32_t* __restrict__ plabel) {
+    PMA_GRID_STRIDE(p, np) {
+        const uint32_t n = slen[p];
+        uint32_t lab = 0;
+        if (n == 1) lab = rank2id[pool[soff[p]]];
+        else if (n >= 2) lab = group_tid[plateau_group[p]];
+        plabel[p] = lab;
+    }
+}
+
+__global__ void voxel_labels(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ plabel,
+                             size_t n, uint32_t* __restrict__ labels) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t p = pid[v];
+        labels[v] = (p == kNone) ? 0u : plabel[p];
+    }
+}
+
+// Old -> new label remap by binary search in sorted old ids.
+__global__ void remap_labels(uint32_t* __restrict__ labels, size_t n, const uint32_t* __restrict__ old_ids,
+                             const uint32_t* __restrict__ new_ids, uint32_t m) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t l = labels[v];
+        if (l == 0) continue;
+        uint32_t lo = 0, hi = m;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (old_ids[mid] < l) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < m && old_ids[lo] == l) labels[v] = new_ids[lo];
+    }
+}
+
+__global__ void to_group_index(const uint32_t* __restrict__ excl, const uint32_t* start, size_t m,
+                               uint32_t* out) {
+    PMA_GRID_STRIDE(i, m) out[i] = excl[i] + start[i] - 1u;
+}
+
+__global__ void gather_lists(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
+                             const uint32_t* __restrict__ pool, const uint32_t* __restrict__ rep,
+                             const unsigned long long* __restrict__ roff, size_t ng,
+                             uint32_t* __restrict__ out) {
+    PMA_GRID_STRIDE(gi, ng) {
+        const uint32_t p = rep[gi];
+        for (uint32_t k = 0; k < slen[p]; ++k) out[roff[gi] + k] = pool[soff[p] + k];
+    }
+}
+
+struct MaxBall {  // same layout as the reference's Model::MaximumBall (Types.h:182-186)
+    int center[3];
+    uint32_t r2;
+};
+
+struct MaxBallDescending {  // Types.h:188-195
+    bool operator()(const MaxBall& a, const MaxBall& b) const { return a.r2 > b.r2; }
+};
+
+template <class T>
+T* buf(pma_ctx* ctx, const char* tag, size_t count) {
+    return static_cast<T*>(ctx->scratch(tag, std::max<size_t>(count, 1) * sizeof(T)));
+}
+
+}  // namespace
+
+pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const uint32_t* crad2,
+                 pma_dims d, pma_stencil st, uint32_t* labels) {
+    check_dims(d);
+    PMA_REQUIRE(mask && edt2 && crad2 && labels, PMA_ERR_ARGUMENT, "pma_pores: null device pointer");
+    cudaStream_t s = ctx->stream;
+    const size_t n = voxels(d);
+    const Grid g{d.sx, d.sy, d.sz};
+    const int d3q7 = st == PMA_D3Q7 ? 1 : 0;
+    const unsigned G = grid_for(ctx, n);
+    int64_t* d_count = buf<int64_t>(ctx, "pores.count", 4);
+    unsigned int* err = reinterpret_cast<unsigned int*>(d_count + 2);
+    PMA_CUDA(cudaMemsetAsync(d_count, 0, 32, s));
+
+    // a8: maximum balls in z, x, y scan order (PoreAndThroatComputer.cpp:93-119) = linear order.
+    uint8_t* flags = buf<uint8_t>(ctx, "pores.flags", n);
+    flag_outer<<<G, 256, 0, s>>>(mask, n, flags);
+    ctx->check_launch("flag_outer");
+    uint32_t* balls = buf<uint32_t>(ctx, "pores.balls", n);
+    const int64_t nb = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), flags, balls,
+                                      static_cast<int64_t>(n), d_count);
+    uint32_t* ball_r2 = buf<uint32_t>(ctx, "pores.ball_r2", nb);
+    if (nb) {
+        gather_u32<<<grid_for(ctx, nb), 256, 0, s>>>(edt2, balls, nb, ball_r2);
+        ctx->check_launch("gather_u32");
+    }
+    std::vector<uint32_t> h_idx(nb), h_r2(nb);
+    if (nb) {
+        PMA_CUDA(cudaMemcpyAsync(h_idx.data(), balls, nb * 4, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(h_r2.data(), ball_r2, nb * 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+    }
+    // std::sort with the reference's comparator (PoreAndThroatComputer.cpp:121-122).
+    std::vector<MaxBall> mb(nb);
+    for (int64_t i = 0; i < nb; ++i) {
+        int x, y, z;
+        g.coords(h_idx[i], x, y, z);
+        mb[i].center[0] = x;
+        mb[i].center[1] = y;
+        mb[i].center[2] = z;
+        mb[i].r2 = h_r2[i];
+    }
+    std::sort(mb.begin(), mb.end(), MaxBallDescending());
+    std::vector<uint32_t> voxel_of_rank(nb);
+    for (int64_t r = 0; r < nb; ++r)
+        voxel_of_rank[r] = static_cast<uint32_t>(g.idx(mb[r].center[0], mb[r].center[1], mb[r].center[2]));
+    uint32_t* crank = buf<uint32_t>(ctx, "pores.crank", n);
+    fill_u32<<<G, 256, 0, s>>>(crank, n, kNone);
+    ctx->check_launch("fill_u32");
+    if (nb) {
+        PMA_CUDA(cudaMemcpyAsync(balls, voxel_of_rank.data(), nb * 4, cudaMemcpyHostToDevice, s));
+        scatter_rank<<<grid_for(ctx, nb), 256, 0, s>>>(balls, nb, crank);
+        ctx->check_launch("scatter_rank");
+    }
+
+    // Plateaus: connected sets of equal crad under the stencil.
+    uint32_t* pid = buf<uint32_t>(ctx, "pores.pid", n);  // root voxel, then plateau id
+    uf_init<<<G, 256, 0, s>>>(crad2, n, pid);
+    ctx->check_launch("uf_init");
+    {
+        KernelTimer kt(ctx, "uf_hook");
+        uf_hook<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid, err);
+    }
+    ctx->check_launch("uf_hook");
+    uf_flatten<<<G, 256, 0, s>>>(n, pid);
+    ctx->check_launch("uf_flatten");
+    flag_roots<<<G, 256, 0, s>>>(pid, n, flags);
+    ctx->check_launch("flag_roots");
+    uint32_t* roots = buf<uint32_t>(ctx, "pores.roots", n);
+    const int64_t np = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), flags, roots,
+                                      static_cast<int64_t>(n), d_count);
+    if (np) {
+        scatter_pid<<<grid_for(ctx, np), 256, 0, s>>>(roots, np, labels);  // labels as scratch
+        ctx->check_launch("scatter_pid");
+        to_pid<<<G, 256, 0, s>>>(labels, n, pid);
+        ctx->check_launch("to_pid");
+    }
+    uint32_t* pcrad = buf<uint32_t>(ctx, "pores.pcrad", np);
+    unsigned int* psize = buf<unsigned int>(ctx, "pores.psize", np);
+    unsigned int* pface = buf<unsigned int>(ctx, "pores.pface", np);
+    uint32_t* pminrank = buf<uint32_t>(ctx, "pores.pminrank", np);
+    PMA_CUDA(cudaMemsetAsync(psize, 0, std::max<int64_t>(np, 1) * 4, s));
+    PMA_CUDA(cudaMemsetAsync(pface, 0, std::max<int64_t>(np, 1) * 4, s));
+    fill_u32<<<grid_for(ctx, np), 256, 0, s>>>(pminrank, np, kNone);
+    ctx->check_launch("fill_u32");
+    plateau_stats<<<G, 256, 0, s>>>(pid, crad2, crank, g, n, pcrad, psize, pface, pminrank);
+    ctx->check_launch("plateau_stats");
+
+    // Edges between plateaus, sorted by destination.
+    auto* ecount = reinterpret_cast<unsigned long long*>(d_count + 1);
+    PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
+    plateau_edges<false><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, nullptr, 0);
+    ctx->check_launch("plateau_edges(count)");
+    unsigned long long ne_raw = 0;
+    PMA_CUDA(cudaMemcpyAsync(&ne_raw, ecount, 8, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    auto* edges_raw = buf<unsigned long long>(ctx, "pores.edges_raw", ne_raw);
+    auto* edges = buf<unsigned long long>(ctx, "pores.edges", ne_raw);
+    PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
+    plateau_edges<true><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, edges_raw, ne_raw);
+    ctx->check_launch("plateau_edges(write)");
+    // Keys are (destination << 32 | source): sorting groups the predecessors of each plateau.
+    int64_t ne = 0;
+    if (ne_raw) {
+        sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_raw));
+        ne = unique(ctx, edges, edges_raw, static_cast<int64_t>(ne_raw), d_count);
+    }
+    unsigned long long* by_dst = edges_raw;
+    unsigned int* eoff = buf<unsigned int>(ctx, "pores.eoff", np + 1);
+    PMA_CUDA(cudaMemsetAsync(eoff, 0, (np + 1) * 4, s));
+    edge_offsets<<<grid_for(ctx, ne + 1), 256, 0, s>>>(by_dst, ne, np, eoff);
+    ctx->check_launch("edge_offsets");
+
+    // Levels: plateaus in decreasing crad.
+    uint32_t* lkey = buf<uint32_t>(ctx, "pores.lkey", np);
+    uint32_t* lval = buf<uint32_t>(ctx, "pores.lval", np);
+    uint32_t* lkey2 = buf<uint32_t>(ctx, "pores.lkey2", np);
+    uint32_t* order = buf<uint32_t>(ctx, "pores.order", np);
+    std::vector<size_t> level_begin;
+    if (np) {
+        level_keys<<<grid_for(ctx, np), 256, 0, s>>>(pcrad, np, lkey, lval);
+        ctx->check_launch("level_keys");
+        sort_pairs(ctx, lkey, lkey2, lval, order, np);
+        std::vector<uint32_t> hk(np);
+        PMA_CUDA(cudaMemcpyAsync(hk.data(), lkey2, np * 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        for (int64_t i = 0; i < np; ++i)
+            if (i == 0 || hk[i] != hk[i - 1]) level_begin.push_back(static_cast<size_t>(i));
+    }
+    level_begin.push_back(static_cast<size_t>(np));
+
+    // Level sweep.
+    size_t max_level = 1;
+    for (size_t l = 0; l + 1 < level_begin.size(); ++l)
+        max_level = std::max(max_level, level_begin[l + 1] - level_begin[l]);
+    PlateauSets ps;
+    ps.eoff = eoff;
+    ps.edges = by_dst;
+    ps.minrank = pminrank;
+    ps.m = buf<uint32_t>(ctx, "pores.m", np);
+    ps.seed = buf<uint32_t>(ctx, "pores.seed", np);
+    ps.soff = buf<unsigned long long>(ctx, "pores.soff", np);
+    ps.slen = buf<uint32_t>(ctx, "pores.slen", np);
+    ps.err = err;
+    unsigned long long* cnt = buf<unsigned long long>(ctx, "pores.cnt", max_level);
+    unsigned long long* off = buf<unsigned long long>(ctx, "pores.off", max_level);
+    unsigned long long* base = reinterpret_cast<unsigned long long*>(d_count + 3);
+    unsigned long long pool_cap = std::max<unsigned long long>(1ull << 20, 24ull * np);
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        ps.pool = buf<uint32_t>(ctx, "pores.pool", pool_cap);
+        ps.pool_cap = pool_cap;
+        PMA_CUDA(cudaMemsetAsync(base, 0, 8, s));
+        PMA_CUDA(cudaMemsetAsync(err, 0, 4, s));
+        KernelTimer kt(ctx, "level_sets");
+        for (size_t l = 0; l + 1 < level_begin.size(); ++l) {
+            const size_t b = level_begin[l], e = level_begin[l + 1];
+            const unsigned lg = grid_for(ctx, e - b, 128);
+            level_sets<false><<<lg, 128, 0, s>>>(ps, order, b, e, cnt, nullptr, nullptr);
+            exclusive_sum(ctx, cnt, off, static_cast<int64_t>(e - b));
+            level_sets<true><<<lg, 128, 0, s>>>(ps, order, b, e, cnt, off, base);
+            level_advance<<<1, 32, 0, s>>>(base, off, cnt, e - b);
+            ctx->count_launch(3);
+        }
+        ctx->check_launch("level_sets");
+        unsigned int h_err = 0;
+        unsigned long long used = 0;
+        PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(&used, base, 8, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        PMA_REQUIRE(!(h_err & 1u), PMA_ERR_LIMIT, "pma_pores: plateau union-find did not converge");
+        if (!(h_err & 2u)) break;
+        PMA_REQUIRE(attempt < 2, PMA_ERR_MEMORY, "pma_pores: seed-set pool overflow");
+        pool_cap = used + (used >> 2) + 1024;
+    }
+
+    // Seeds -> pores in rank order.
+    std::vector<uint32_t> h_seed(np);
+    if (np) PMA_CUDA(cudaMemcpyAsync(h_seed.data(), ps.seed, np * 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    std::vector<uint32_t> seed_ranks;
+    for (int64_t p = 0; p < np; ++p)
+        if (h_seed[p] != kNone) seed_ranks.push_back(h_seed[p]);
+    std::sort(seed_ranks.begin(), seed_ranks.end());
+    const size_t npores = seed_ranks.size();
+    const std::vector<uint32_t> ids = pore_id_sequence(npores);
+    std::vector<uint32_t> rank2pore(std::max<int64_t>(nb, 1), kNone), rank2id(std::max<int64_t>(nb, 1), 0);
+    for (size_t k = 0; k < npores; ++k) {
+        rank2pore[seed_ranks[k]] = static_cast<uint32_t>(k);
+        rank2id[seed_ranks[k]] = ids[k];
+    }
+    uint32_t* d_rank2pore = buf<uint32_t>(ctx, "pores.rank2pore", rank2pore.size());
+    uint32_t* d_rank2id = buf<uint32_t>(ctx, "pores.rank2id", rank2id.size());
+    PMA_CUDA(cudaMemcpyAsync(d_rank2pore, rank2pore.data(), rank2pore.size() * 4, cudaMemcpyHostToDevice, s));
+    PMA_CUDA(cudaMemcpyAsync(d_rank2id, rank2id.data(), rank2id.size() * 4, cudaMemcpyHostToDevice, s));
+    PoreAcc pa;
+    pa.rank2pore = d_rank2pore;
+    pa.pvol = buf<unsigned long long>(ctx, "pores.pvol", npores);
+    pa.pbound = buf<unsigned int>(ctx, "pores.pbound", npores);
+    PMA_CUDA(cudaMemsetAsync(pa.pvol, 0, std::max<size_t>(npores, 1) * 8, s));
+    PMA_CUDA(cudaMemsetAsync(pa.pbound, 0, std::max<size_t>(npores, 1) * 4, s));
+    if (np) {
+        pore_accumulate<<<grid_for(ctx, np), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, psize, pface, np, pa);
+        ctx->check_launch("pore_accumulate");
+    }
+
+    // Throats: plateaus with two or more seeds, grouped by equal seed sets.
+    if (np) {
+        flag_multi<<<grid_for(ctx, np), 256, 0, s>>>(ps.slen, np, flags);
+        ctx->check_launch("flag_multi");
+    }
+    uint32_t* multi = buf<uint32_t>(ctx, "pores.multi", np);
+    const int64_t nm = np ? select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), flags, multi,
+                                           np, d_count)
+                          : 0;
+    std::vector<uint32_t> group_tid_h;
+    uint32_t* plateau_group = buf<uint32_t>(ctx, "pores.pgroup", np);
+    uint32_t* group_tid = nullptr;
+    pma_table* t = new pma_table;
+    std::vector<unsigned long long> h_gvol, h_gfirst;
+    std::vector<uint32_t> h_grep;
+    std::vector<std::vector<uint32_t>> glist;
+    int64_t ngroups = 0;
+    if (nm) {
+        auto* h1 = buf<unsigned long long>(ctx, "pores.h1", nm);
+        auto* h2 = buf<unsigned long long>(ctx, "pores.h2", nm);
+        auto* ktmp = buf<unsigned long long>(ctx, "pores.ktmp", nm);
+        uint32_t* v1 = buf<uint32_t>(ctx, "pores.v1", nm);
+        uint32_t* v2 = buf<uint32_t>(ctx, "pores.v2", nm);
+        // Group plateaus with equal seed sets: stable radix sorts by h2 then by h1, so equal
+        // (h1, h2) pairs end up adjacent.
+        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, multi, nm, h1, h2);
+        ctx->check_launch("throat_hashes");
+        sort_pairs(ctx, h2, ktmp, multi, v1, nm);
+        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v1, nm, h1, h2);
+        ctx->check_launch("throat_hashes");
+        sort_pairs(ctx, h1, ktmp, v1, v2, nm);
+        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v2, nm, h1, h2);
+        ctx->check_launch("throat_hashes");
+        uint32_t* gstart = buf<uint32_t>(ctx, "pores.gstart", nm);
+        uint32_t* gid = buf<uint32_t>(ctx, "pores.gid", nm);
+        group_starts<<<grid_for(ctx, nm), 256, 0, s>>>(v2, h1, h2, nm, ps.soff, ps.slen, ps.pool, gstart, err);
+        ctx->check_launch("group_starts");
+        exclusive_sum(ctx, gstart, gid, nm);
+        uint32_t last_off = 0, last_start = 0;
+        PMA_CUDA(cudaMemcpyAsync(&last_off, gid + nm - 1, 4, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(&last_start, gstart + nm - 1, 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        ngroups = static_cast<int64_t>(last_off) + last_start;
+        to_group_index<<<grid_for(ctx, nm), 256, 0, s>>>(gid, gstart, nm, gstart);
+        ctx->check_launch("to_group_index");
+        GroupOut go;
+        go.gvol = buf<unsigned long long>(ctx, "pores.gvol", ngroups);
+        go.gfirst = buf<unsigned long long>(ctx, "pores.gfirst", ngroups);
+        go.grep = buf<uint32_t>(ctx, "pores.grep", ngroups);
+        go.group_of = nullptr;
+        PMA_CUDA(cudaMemsetAsync(go.gvol, 0, ngroups * 8, s));
+        PMA_CUDA(cudaMemsetAsync(go.gfirst, 0xFF, ngroups * 8, s));
+        group_reduce<<<grid_for(ctx, nm), 256, 0, s>>>(v2, gstart, nm, psize, roots, go, plateau_group);
+        ctx->check_launch("group_reduce");
+        h_gvol.resize(ngroups);
+        h_gfirst.resize(ngroups);
+        h_grep.resize(ngroups);
+        PMA_CUDA(cudaMemcpyAsync(h_gvol.data(), go.gvol, ngroups * 8, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(h_gfirst.data(), go.gfirst, ngroups * 8, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(h_grep.data(), go.grep, ngroups * 4, cudaMemcpyDeviceToHost, s));
+        unsigned int h_err = 0;
+        PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        PMA_REQUIRE(!(h_err & 4u), PMA_ERR_INTERNAL, "pma_pores: seed-set hash collision");
+        // Representative seed lists, gathered into one buffer.
+        std::vector<uint32_t> rlen(ngroups);
+        uint32_t* d_rep_len = buf<uint32_t>(ctx, "pores.rlen", ngroups);
+        gather_u32<<<grid_for(ctx, ngroups), 256, 0, s>>>(ps.slen, go.grep, ngroups, d_rep_len);
+        ctx->check_launch("gather_u32");
+        PMA_CUDA(cudaMemcpyAsync(rlen.data(), d_rep_len, ngroups * 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        std::vector<unsigned long long> roff(ngroups + 1, 0);
+        for (int64_t gi = 0; gi < ngroups; ++gi) roff[gi + 1] = roff[gi] + rlen[gi];
+        auto* d_roff = buf<unsigned long long>(ctx, "pores.roff", ngroups + 1);
+        uint32_t* d_rlist = buf<uint32_t>(ctx, "pores.rlist", roff[ngroups]);
+        PMA_CUDA(cudaMemcpyAsync(d_roff, roff.data(), (ngroups + 1) * 8, cudaMemcpyHostToDevice, s));
+        gather_lists<<<grid_for(ctx, ngroups), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, go.grep, d_roff,
+                                                            ngroups, d_rlist);
+        ctx->check_launch("gather_lists");
+        std::vector<uint32_t> flat(roff[ngroups]);
+        PMA_CUDA(cudaMemcpyAsync(flat.data(), d_rlist, flat.size() * 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        glist.resize(ngroups);
+        for (int64_t gi = 0; gi < ngroups; ++gi)
+            glist[gi].assign(flat.begin() + roff[gi], flat.begin() + roff[gi + 1]);
+    }
+    // Throat ids: order by (last pore of the type, first voxel), counting down from
+    // UINT32_MAX - 1 (BasePoreAndThroatComputer.cpp:122-130).
+    std::vector<int64_t> gorder(ngroups);
+    for (int64_t i = 0; i < ngroups; ++i) gorder[i] = i;
+    std::sort(gorder.begin(), gorder.end(), [&](int64_t a, int64_t b) {
+        const uint32_t la = glist[a].back(), lb = glist[b].back();
+        if (la != lb) return la < lb;
+        return h_gfirst[a] < h_gfirst[b];
+    });
+    group_tid_h.assign(std::max<int64_t>(ngroups, 1), 0);
+    for (int64_t k = 0; k < ngroups; ++k) group_tid_h[gorder[k]] = 0xFFFFFFFFu - 1u - static_cast<uint32_t>(k);
+    group_tid = buf<uint32_t>(ctx, "pores.gtid", group_tid_h.size());
+    PMA_CUDA(cudaMemcpyAsync(group_tid, group_tid_h.data(), group_tid_h.size() * 4, cudaMemcpyHostToDevice, s));
+
+    // Labels.
+    uint32_t* plabel = buf<uint32_t>(ctx, "pores.plabel", np);
+    if (np) {
+        plateau_labels<<<grid_for(ctx, np), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, d_rank2id, plateau_group,
+                                                         group_tid, np, plabel);
+        ctx->check_launch("plateau_labels");
+    }
+    voxel_labels<<<G, 256, 0, s>>>(pid, plabel, n, labels);
+    ctx->check_launch("voxel_labels");
+
+    // Table (pores in id order, throats in id order).
+    std::vector<unsigned long long> pvol(npores);
+    std::vector<unsigned int> pbound(npores);
+    if (npores) {
+        PMA_CUDA(cudaMemcpyAsync(pvol.data(), pa.pvol, npores * 8, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(pbound.data(), pa.pbound, npores * 4, cudaMemcpyDeviceToHost, s));
+    }
+    ctx->sync();
+    for (size_t k = 0; k < npores; ++k) {
+        const MaxBall& b = mb[seed_ranks[k]];
+        pma_pore p;
+        std::memset(&p, 0, sizeof(p));
+        p.id = ids[k];
+        p.seed_x = b.center[0];
+        p.seed_y = b.center[1];
+        p.seed_z = b.center[2];
+        p.seed_r2 = b.r2;
+        p.is_boundary = pbound[k] ? 1 : 0;
+        p.volume = pvol[k];
+        t->pores.push_back(p);
+    }
+    // Throat rows: pore list in processing order [second, first, third, ...]
+    // (BasePoreAndThroatComputer.cpp:338-340, 370-371), sorted by id.
+    std::vector<int64_t> by_id(ngroups);
+    for (int64_t k = 0; k < ngroups; ++k) by_id[k] = gorder[ngroups - 1 - k];
+    for (int64_t gi : by_id) {
+        pma_throat th;
+        th.id = group_tid_h[gi];
+        th.volume = h_gvol[gi];
+        th.pool_offset = t->pool.size();
+        const std::vector<uint32_t>& L = glist[gi];
+        th.n_pores = static_cast<uint32_t>(L.size());
+        t->pool.push_back(rank2id[L[1]]);
+        t->pool.push_back(rank2id[L[0]]);
+        for (size_t k = 2; k < L.size(); ++k) t->pool.push_back(rank2id[L[k]]);
+        t->throats.push_back(th);
+    }
+    return t;
+}
+
+// a11: EmptyPoresRemover.cpp:31-244 on the host table, then one relabel launch.
+void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d) {
+    check_dims(d);
+    PMA_REQUIRE(labels, PMA_ERR_ARGUMENT, "pma_remove_empty_pores: null labels");
+    std::map<uint32_t, uint32_t> remap;
+    // EPR.cpp:193-244: drop zero-volume pores and remove them from the type lists.
+    std::vector<uint32_t> empty;
+    std::vector<pma_pore> kept;
+    for (const pma_pore& p : t->pores) {
+        if (p.volume == 0) empty.push_back(p.id);
+        else kept.push_back(p);
+    }
+    std::sort(empty.begin(), empty.end());
+    struct Row {
+        uint32_t id;
+        uint64_t volume;
+        std::vector<uint32_t> pores;
+    };
+    std::map<uint32_t, Row> rows;
+    for (const pma_throat& th : t->throats) {
+        Row r;
+        r.id = th.id;
+        r.volume = th.volume;
+        r.pores.assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
+        std::sort(r.pores.begin(), r.pores.end());
+        std::vector<uint32_t> k;
+        std::set_difference(r.pores.begin(), r.pores.end(), empty.begin(), empty.end(), std::back_inserter(k));
+        r.pores = k;
+        rows[r.id] = r;
+    }
+    // EPR.cpp:167-191: types with fewer than two pores.
+    std::vector<uint32_t> few;
+    for (auto& kv : rows)
+        if (kv.second.pores.size() < 2) few.push_back(kv.first);
+    for (uint32_t id : few) {
+        if (rows[id].pores.size() == 1) remap[id] = rows[id].pores[0];
+        rows.erase(id);
+    }
+    // EPR.cpp:126-165: merge duplicates into the largest id.
+    std::map<std::vector<uint32_t>, std::vector<uint32_t>> by_pores;
+    for (auto& kv : rows) by_pores[kv.second.pores].push_back(kv.first);
+    for (auto& kv : by_pores) {
+        const std::vector<uint32_t>& idsv = kv.second;
+        if (idsv.size() < 2) continue;
+        const uint32_t keep = *std::max_element(idsv.begin(), idsv.end());
+        for (uint32_t id : idsv)
+            if (id != keep) {
+                rows.erase(id);
+                remap[id] = keep;
+            }
+    }
+    t->pores = kept;
+    t->throats.clear();
+    t->pool.clear();
+    for (auto& kv : rows) {
+        pma_throat th;
+        th.id = kv.first;
+        th.volume = kv.second.volume;
+        th.n_pores = static_cast<uint32_t>(kv.second.pores.size());
+        th.pool_offset = t->pool.size();
+        t->pool.insert(t->pool.end(), kv.second.pores.begin(), kv.second.pores.end());
+        t->throats.push_back(th);
+    }
+    if (remap.empty()) return;  // EPR.cpp:54-57
+    std::vector<uint32_t> o, nw;
+    for (auto& kv : remap) {
+        o.push_back(kv.first);
+        nw.push_back(kv.second);
+    }
+    cudaStream_t s = ctx->stream;
+    uint32_t* d_old = buf<uint32_t>(ctx, "remove.old", o.size());
+    uint32_t* d_new = buf<uint32_t>(ctx, "remove.new", nw.size());
+    PMA_CUDA(cudaMemcpyAsync(d_old, o.data(), o.size() * 4, cudaMemcpyHostToDevice, s));
+    PMA_CUDA(cudaMemcpyAsync(d_new, nw.data(), nw.size() * 4, cudaMemcpyHostToDevice, s));
+    const size_t n = voxels(d);
+    remap_labels<<<grid_for(ctx, n), 256, 0, s>>>(labels, n, d_old, d_new, static_cast<uint32_t>(o.size()));
+    ctx->check_launch("remap_labels");
+    ctx->sync();
 }
 
 }  // namespace pma

@@ -91,11 +91,20 @@ def grf(shape=(512, 512, 512), sigma=3.0, porosity=0.65, seed=2, device=None):
     k = torch.exp(-0.5 * (xs / sigma) ** 2)
     k = (k / k.sum()).view(1, 1, -1)
     for axis in range(3):
-        f = f.movedim(axis, -1)
+        f = f.movedim(axis, -1).contiguous()
         s = f.shape
-        flat = f.reshape(-1, 1, s[-1])
-        flat = torch.nn.functional.pad(flat, (rad, rad), mode="reflect")
-        f = torch.nn.functional.conv1d(flat, k).reshape(s).movedim(-1, axis)
+        n = s[-1]
+        # reflect padding ("reflect" mode of scipy.ndimage: the edge sample is repeated)
+        left = torch.arange(rad - 1, -1, -1, device=device).clamp(max=n - 1)
+        right = torch.arange(n - 1, n - 1 - rad, -1, device=device).clamp(min=0)
+        idx = torch.cat([left, torch.arange(n, device=device), right])
+        flat = f.reshape(-1, n)
+        out = torch.empty_like(flat)
+        step = 1 << 15
+        for r0 in range(0, flat.shape[0], step):
+            blk = flat[r0:r0 + step].index_select(1, idx).unsqueeze(1)
+            out[r0:r0 + step] = torch.nn.functional.conv1d(blk, k).squeeze(1)
+        f = out.reshape(s).movedim(-1, axis)
     idx = torch.randint(0, f.numel(), (1 << 24,), generator=g, device=device)
     t = torch.quantile(f.reshape(-1)[idx].double(), 1.0 - porosity).float()
     return (f <= t).to(torch.uint8)
