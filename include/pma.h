@@ -60,7 +60,8 @@ int pma_ctx_set_stream(pma_ctx* ctx, void* cuda_stream);
 uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
 /* Opt-in kernel timing: with timing on, the hot kernels are bracketed by CUDA events on
  * the context's stream. The report is a JSON object {"kernel": [total_ms, launches], ...}
- * of everything timed since the previous report; returns its full length. */
+ * of everything timed since the previous report; each call consumes the timed events, so
+ * pass a buffer large enough for the whole report. Returns its full length. */
 int pma_ctx_set_timing(pma_ctx* ctx, int enable);
 size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap);
 /* Device bytes held by ctx's scratch cache; pma_ctx_trim releases them. */

@@ -54,6 +54,8 @@ def lib():
         l.orc_max_ball_mask.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
         l.orc_pores.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
         l.orc_pores.restype = P
+        l.orc_sorted_balls.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_size_t]
+        l.orc_sorted_balls.restype = ctypes.c_size_t
         l.orc_remove_empty_pores.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         l.orc_watershed.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_uint32, P]
@@ -132,6 +134,17 @@ def _table(h):
     throats = [(tp[i].id, tp[i].volume,
                 tuple(pool[tp[i].pool_offset + j] for j in range(tp[i].n_pores))) for i in range(m)]
     return pores, throats
+
+
+def sorted_balls(mask, edt2):
+    """Linear indices of the maximum balls in the reference's std::sort order."""
+    mask = np.ascontiguousarray(mask, dtype=np.uint8)
+    edt2 = np.ascontiguousarray(edt2, dtype=np.uint32)
+    sx, sy, sz = _dims(edt2)
+    out = np.empty(int((mask == 255).sum()), dtype=np.uint32)
+    n = lib().orc_sorted_balls(_p(mask), _p(edt2), sx, sy, sz, _p(out), out.size)
+    assert n == out.size
+    return out
 
 
 class PoreResult:

@@ -396,6 +396,28 @@ extern "C" orc_table* orc_pores(const uint8_t* mask, const uint32_t* edt2,
     return make_table(st.pores, st.throats);
 }
 
+// The std::sort order of a8 (PoreAndThroatComputer.cpp:93-123): writes the linear index of
+// each maximum ball in sorted order; returns their number.
+extern "C" size_t orc_sorted_balls(const uint8_t* mask, const uint32_t* edt2, int sx, int sy, int sz,
+                                   uint32_t* out, size_t cap) {
+    Dims d{sx, sy, sz};
+    std::vector<MaxBall> balls;
+    for (int z = 0; z < sz; ++z)
+        for (int x = 0; x < sx; ++x)
+            for (int y = 0; y < sy; ++y) {
+                size_t v = d.idx(x, y, z);
+                if (mask[v] != 255) continue;
+                MaxBall b;
+                b.center = {x, y, z};
+                b.r2 = edt2[v];
+                balls.push_back(b);
+            }
+    std::sort(balls.begin(), balls.end(), MaxBallDescending());
+    for (size_t i = 0; i < balls.size() && i < cap; ++i)
+        out[i] = static_cast<uint32_t>(d.idx(balls[i].center[0], balls[i].center[1], balls[i].center[2]));
+    return balls.size();
+}
+
 // a11: EmptyPoresRemover.cpp:31-244.
 extern "C" int orc_remove_empty_pores(orc_table* t, uint32_t* labels, int sx, int sy, int sz) {
     std::map<uint32_t, Pore> pores;

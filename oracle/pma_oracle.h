@@ -74,6 +74,10 @@ int orc_max_ball_mask(const uint32_t* cx, const uint32_t* cy, const uint32_t* cz
 orc_table* orc_pores(const uint8_t* mask, const uint32_t* edt2, const uint32_t* crad2,
                      int sx, int sy, int sz, int d3q7, uint32_t* labels);
 
+/* The maximum balls of a8 in std::sort order (linear indices); returns their number. */
+size_t orc_sorted_balls(const uint8_t* mask, const uint32_t* edt2, int sx, int sy, int sz,
+                        uint32_t* out, size_t cap);
+
 /* a11: empty-pore removal; rewrites the table and remaps labels (EmptyPoresRemover.cpp:31-244). */
 int orc_remove_empty_pores(orc_table* t, uint32_t* labels, int sx, int sy, int sz);
 

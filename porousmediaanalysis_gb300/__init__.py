@@ -70,9 +70,8 @@ class Context:
     def timing_report(self):
         """{kernel: (total_ms, launches)} of timed kernels since the previous report."""
         import json
-        n = capi.lib().pma_ctx_timing_report(self.handle, None, 0)
-        buf = ctypes.create_string_buffer(n + 1)
-        capi.lib().pma_ctx_timing_report(self.handle, buf, n + 1)
+        buf = ctypes.create_string_buffer(1 << 16)  # one call: the report is consumed
+        capi.lib().pma_ctx_timing_report(self.handle, buf, len(buf))
         return {k: tuple(v) for k, v in json.loads(buf.value.decode()).items()}
 
 

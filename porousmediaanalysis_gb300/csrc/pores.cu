@@ -121,9 +121,17 @@ __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int
     }
 }
 
-__global__ void uf_flatten(size_t n, uint32_t* __restrict__ parent) {
+// Read-only root walk: flattening must not halve paths, or a racing halving store could
+// replace another voxel's final root pointer with an intermediate ancestor.
+__device__ __forceinline__ uint32_t uf_root_readonly(const uint32_t* parent, uint32_t v) {
+    uint32_t cur = v, next;
+    while ((next = parent[cur]) != cur) cur = next;
+    return cur;
+}
+
+__global__ void uf_flatten(size_t n, uint32_t* parent) {
     PMA_GRID_STRIDE(v, n) {
-        if (parent[v] != kNone) parent[v] = uf_root(parent, static_cast<uint32_t>(v));
+        if (parent[v] != kNone) parent[v] = uf_root_readonly(parent, static_cast<uint32_t>(v));
     }
 }
 
@@ -136,10 +144,18 @@ __global__ void scatter_pid(const uint32_t* __restrict__ roots, size_t np, uint3
 }
 
 // parent[v] (the root voxel) becomes the dense plateau id.
-__global__ void to_pid(const uint32_t* __restrict__ tmp, size_t n, uint32_t* __restrict__ parent) {
+__global__ void to_pid(const uint32_t* __restrict__ tmp, size_t n, size_t np, uint32_t* __restrict__ parent,
+                       unsigned int* __restrict__ err) {
     PMA_GRID_STRIDE(v, n) {
         const uint32_t r = parent[v];
-        if (r != kNone) parent[v] = tmp[r];
+        if (r == kNone) continue;
+        const uint32_t p = tmp[r];
+        if (p < np) {
+            parent[v] = p;
+        } else {  // not a root: refuse rather than index past the plateau arrays
+            parent[v] = kNone;
+            atomicOr(err, 8u);
+        }
     }
 }
 
@@ -286,8 +302,11 @@ __global__ void level_sets(PlateauSets st, const uint32_t* __restrict__ order, s
             last = best;
         }
         if (kWrite) {
-            st.soff[p] = pos;
-            st.slen[p] = static_cast<uint32_t>(k);
+            // A list that did not fit is recorded empty so later levels never read past the
+            // pool; the overflow flag makes the host redo the sweep with a larger pool.
+            const bool fits = pos + k <= st.pool_cap;
+            st.soff[p] = fits ? pos : 0;
+            st.slen[p] = fits ? static_cast<uint32_t>(k) : 0u;
         } else {
             cnt[i - begin] = k;
         }
@@ -527,8 +546,12 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     if (np) {
         scatter_pid<<<grid_for(ctx, np), 256, 0, s>>>(roots, np, labels);  // labels as scratch
         ctx->check_launch("scatter_pid");
-        to_pid<<<G, 256, 0, s>>>(labels, n, pid);
+        to_pid<<<G, 256, 0, s>>>(labels, n, np, pid, err);
         ctx->check_launch("to_pid");
+        unsigned int h_err = 0;
+        PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        PMA_REQUIRE(!(h_err & 8u), PMA_ERR_INTERNAL, "pma_pores: plateau labelling left a non-root parent");
     }
     uint32_t* pcrad = buf<uint32_t>(ctx, "pores.pcrad", np);
     unsigned int* psize = buf<unsigned int>(ctx, "pores.psize", np);
@@ -600,7 +623,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     unsigned long long* cnt = buf<unsigned long long>(ctx, "pores.cnt", max_level);
     unsigned long long* off = buf<unsigned long long>(ctx, "pores.off", max_level);
     unsigned long long* base = reinterpret_cast<unsigned long long*>(d_count + 3);
-    unsigned long long pool_cap = std::max<unsigned long long>(1ull << 20, 24ull * np);
+    unsigned long long pool_cap = std::max<unsigned long long>(1ull << 22, 32ull * np);
     for (int attempt = 0; attempt < 3; ++attempt) {
         ps.pool = buf<uint32_t>(ctx, "pores.pool", pool_cap);
         ps.pool_cap = pool_cap;

@@ -11,7 +11,7 @@ import pytest
 
 from cases import QUICK, load_example, make_case
 from conftest import GOLDEN
-from util import cavity_key, digest, rows
+from util import cavity_key, digest, rows, trimmed_hist
 
 FIELD_OF = {
     "EuclideanDistanceSquares": "edt2", "ContainingBallRadiiSquares": "crad2",
@@ -50,10 +50,7 @@ def test_oracle_matches_reference_cases(oracle_mod, ref_cases, name):
 def test_oracle_histogram_matches_reference(oracle_mod, ref_cases):
     vol, _ = make_case("union_small")
     _, mx, hist = oracle_mod.edt(vol)
-    h = list(hist)
-    nz = [i for i, v in enumerate(h) if v]
-    trimmed = h[1:nz[-1] + 2] if nz else []
-    assert [int(v) for v in trimmed] == ref_cases["union_small"]["hist"]
+    assert trimmed_hist(hist) == ref_cases["union_small"]["hist"]
 
 
 def test_oracle_matches_shipped_example(oracle_mod, example_golden):
@@ -64,9 +61,7 @@ def test_oracle_matches_shipped_example(oracle_mod, example_golden):
     e, mx, hist = oracle_mod.edt(solid)
     assert digest(e) == ship["digests"]["EuclideanDistanceSquares"]
     assert mx == ship["max_edt2"] == 2561
-    h = [int(v) for v in hist]
-    nz = [i for i, v in enumerate(h) if v]
-    assert h[1:nz[-1] + 2] == ship["hist"]
+    assert trimmed_hist(hist) == ship["hist"]
     crad2, cx, cy, cz = oracle_mod.containing_balls(e, mx)
     assert digest(crad2) == ship["digests"]["ContainingBallRadiiSquares"]
     d, cav, cavities = oracle_mod.geodesic(solid)

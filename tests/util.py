@@ -16,6 +16,14 @@ def rows(x):
     return out
 
 
+def trimmed_hist(hist):
+    """The histogram lines euclideanDistanceSquareCounts.txt holds: entries 1 .. last non-zero,
+    plus one zero (EuclideanDistanceComputer.cpp:83-110, Serializer.cpp:148-159)."""
+    h = [int(v) for v in hist] + [0]
+    nz = [i for i, v in enumerate(h) if v]
+    return h[1:nz[-1] + 2] if nz else []
+
+
 def cavity_key(c):
     """Cavity row without the printed float (compared separately at %f precision)."""
     return (c[0], c[1], c[2], c[3], c[5], c[6], c[7])
