@@ -6,22 +6,33 @@
 // ends with the largest r^2 covering it and, among those, the lexicographically smallest
 // (x, y, z) centre. Both orders fit one 64-bit key,
 //     key = (r^2 << 32) | (0xFFFFFFFF - ((x * SY + y) * SZ + z)),
-// and the result is the atomicMax of keys over covering balls, whatever the order.
+// and the winner of a voxel is the covering centre of largest key.
 //
 // Work reduction: a centre whose discrete ball lies inside the ball of one of its 26
 // neighbours can never win a voxel (the neighbour covers the same voxels with a strictly
-// larger radius), so it is not scattered. Containment B(c, R) in B(c + e, R') holds iff
-// R' >= M_k(R) = max over lattice v with |v|^2 <= R of |v + e|^2, k = |e|^2; the table
-// M_k is computed exactly for R <= kExactTable and replaced above it by the continuous
-// sufficient condition (sqrt(R) + sqrt(k))^2 <= R'. Surviving centres are bucketed by
-// r^2 and scattered largest first, so most reads find a larger key already in place and
-// skip the atomic.
-#include "pma_internal.h"
+// larger radius), so it is dropped. Containment B(c, R) in B(c + e, R') holds iff
+// R' >= M_k(R) = max over lattice v with |v|^2 <= R of |v + e|^2, k = |e|^2; M_k is computed
+// exactly for R < kExactTable and replaced above it by the continuous sufficient condition
+// (sqrt(R) + sqrt(k))^2 <= R'.
+//
+// Gather: the volume is cut into 8^3 tiles; every kept centre is listed in each tile its
+// ball reaches. One CTA per tile sorts its list by key in shared memory (descending), and
+// each voxel takes the first entry whose ball covers it: that entry is the covering centre
+// of largest key, i.e. the reference's winner. A voxel stops at its winner, so the work is
+// the winner's rank in the tile list rather than the ball volumes a scatter would touch.
+#include <thrust/iterator/counting_iterator.h>
+
+#include <vector>
+
+#include "devutil.cuh"
 
 namespace pma {
 namespace {
 
 constexpr uint32_t kExactTable = 1u << 16;
+constexpr int kTile = 8;          // tile edge
+constexpr int kTileVox = 512;     // voxels (and threads) per tile
+constexpr int kListCap = 2048;    // entries sorted in shared memory; longer lists go in chunks
 
 __device__ __forceinline__ uint32_t isqrt_u32(uint32_t n) {
     uint32_t r = static_cast<uint32_t>(sqrtf(static_cast<float>(n)));
@@ -55,14 +66,7 @@ __global__ void balls_containment_table(uint32_t* __restrict__ m1, uint32_t* __r
     m3[R] = b3;
 }
 
-struct Geo {
-    int SX, SY, SZ;
-    __device__ __forceinline__ size_t idx(int x, int y, int z) const {
-        return (static_cast<size_t>(z) * SX + x) * SY + y;
-    }
-};
-
-__device__ __forceinline__ bool dominated(const uint32_t* __restrict__ edt2, Geo g, int x, int y,
+__device__ __forceinline__ bool dominated(const uint32_t* __restrict__ edt2, Grid g, int x, int y,
                                           int z, uint32_t R, const uint32_t* __restrict__ mtab,
                                           uint32_t ntab) {
     for (int dz = -1; dz <= 1; ++dz) {
@@ -93,119 +97,197 @@ __device__ __forceinline__ bool dominated(const uint32_t* __restrict__ edt2, Geo
     return false;
 }
 
-// Pass 1 (count) and pass 2 (place) of the counting sort of surviving centres by r^2.
-template <bool kPlace>
-__global__ void balls_candidates(const uint32_t* __restrict__ edt2, Geo g, size_t n,
-                                 const uint32_t* __restrict__ mtab, uint32_t ntab, uint32_t nR,
-                                 uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
-                                 uint32_t* __restrict__ list, unsigned long long* __restrict__ keys,
-                                 unsigned int* __restrict__ err) {
-    for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
-         v += static_cast<size_t>(gridDim.x) * blockDim.x) {
+__global__ void balls_candidate_flags(const uint32_t* __restrict__ edt2, Grid g, size_t n,
+                                      const uint32_t* __restrict__ mtab, uint32_t ntab, uint32_t nR,
+                                      uint8_t* __restrict__ flags, unsigned int* __restrict__ err) {
+    PMA_GRID_STRIDE(v, n) {
         const uint32_t R = edt2[v];
-        if (!kPlace) keys[v] = (R == 0) ? ~0ull : 0ull;  // solid voxels never change
-        if (R == 0) continue;
-        if (R >= nR) {  // max_edt2 below the data: refuse rather than index past counts
-            atomicOr(err, 1u);
-            continue;
+        uint8_t f = 0;
+        if (R != 0) {
+            if (R >= nR) {  // max_edt2 below the data: refuse rather than index past the table
+                atomicOr(err, 1u);
+            } else {
+                int x, y, z;
+                g.coords(v, x, y, z);
+                f = dominated(edt2, g, x, y, z, R, mtab, ntab) ? 0 : 1;
+            }
         }
-        const int y = static_cast<int>(v % g.SY);
-        const size_t zx = v / g.SY;
-        const int x = static_cast<int>(zx % g.SX);
-        const int z = static_cast<int>(zx / g.SX);
-        if (dominated(edt2, g, x, y, z, R, mtab, ntab)) continue;
-        if (kPlace) list[atomicAdd(&cursor[R], 1u)] = static_cast<uint32_t>(v);
-        else atomicAdd(&counts[R], 1u);
+        flags[v] = f;
     }
 }
 
-// Exclusive scan of counts in descending r^2 order: cursor[R] = sum of counts[R' > R].
-// One block; nR is at most max_edt2 + 1.
-__global__ void balls_bucket_offsets(const uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
-                                     uint32_t nR, uint32_t* __restrict__ total) {
-    __shared__ unsigned long long part[1024];
-    const uint32_t per = (nR + blockDim.x - 1) / blockDim.x;
-    // thread t owns the descending range [nR-1 - t*per, ...)
-    unsigned long long s = 0;
-    for (uint32_t i = 0; i < per; ++i) {
-        long long R = static_cast<long long>(nR) - 1 - (static_cast<long long>(threadIdx.x) * per + i);
-        if (R >= 0) s += counts[R];
+struct Tiles {
+    int TX, TY, TZ;  // tiles per axis
+    __device__ __forceinline__ size_t id(int tx, int ty, int tz) const {
+        return (static_cast<size_t>(tz) * TX + tx) * TY + ty;
     }
-    part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long run = 0;
-        for (unsigned t = 0; t < blockDim.x; ++t) {
-            unsigned long long c = part[t];
-            part[t] = run;
-            run += c;
-        }
-        *total = static_cast<uint32_t>(run);
-    }
-    __syncthreads();
-    unsigned long long run = part[threadIdx.x];
-    for (uint32_t i = 0; i < per; ++i) {
-        long long R = static_cast<long long>(nR) - 1 - (static_cast<long long>(threadIdx.x) * per + i);
-        if (R >= 0) {
-            cursor[R] = static_cast<uint32_t>(run);
-            run += counts[R];
-        }
-    }
-}
+};
 
-// Scatter: warps take centres in list order (largest r^2 first). Lanes split into groups
-// of G; a group walks one y-span of the ball at a time.
-__global__ void balls_scatter(const uint32_t* __restrict__ edt2, Geo g,
-                              const uint32_t* __restrict__ list, uint32_t total,
-                              unsigned int* __restrict__ next, unsigned long long* __restrict__ keys) {
-    const int lane = threadIdx.x & 31;
-    while (true) {
-        uint32_t item = 0;
-        if (lane == 0) item = atomicAdd(next, 1u);
-        item = __shfl_sync(0xFFFFFFFFu, item, 0);
-        if (item >= total) return;
-        const uint32_t v = list[item];
-        const uint32_t R = edt2[v];
-        const int cy = static_cast<int>(v % g.SY);
-        const size_t zx = v / g.SY;
-        const int cx = static_cast<int>(zx % g.SX);
-        const int cz = static_cast<int>(zx / g.SX);
-        const uint32_t lex = (static_cast<uint32_t>(cx) * g.SY + cy) * static_cast<uint32_t>(g.SZ) + cz;
-        const unsigned long long key = (static_cast<unsigned long long>(R) << 32) | (0xFFFFFFFFu - lex);
-        const int r = static_cast<int>(isqrt_u32(R));
-        const int G = r >= 12 ? 32 : (r >= 6 ? 16 : (r >= 3 ? 8 : 4));
-        const int groups = 32 / G;
-        const int grp = lane / G, gl = lane % G;
-        const int x0 = max(cx - r, 0), x1 = min(cx + r, g.SX - 1);
-        const int z0 = max(cz - r, 0), z1 = min(cz + r, g.SZ - 1);
-        const int nxs = x1 - x0 + 1;
-        const int nspans = nxs * (z1 - z0 + 1);
-        for (int s = grp; s < nspans; s += groups) {
-            const int z = z0 + s / nxs;
-            const int x = x0 + s % nxs;
-            const int ddx = x - cx, ddz = z - cz;
-            const int rem = static_cast<int>(R) - ddx * ddx - ddz * ddz;
-            if (rem < 0) continue;
-            const int w = static_cast<int>(isqrt_u32(static_cast<uint32_t>(rem)));
-            const int ya = max(cy - w, 0), yb = min(cy + w, g.SY - 1);
-            unsigned long long* row = keys + g.idx(x, 0, z);
-            for (int y = ya + gl; y <= yb; y += G) {
-                const unsigned long long cur = __ldcg(row + y);
-                if (cur < key) atomicMax(row + y, key);
+// Visits the tiles whose box is within sqrt(R) of centre (x, y, z), restricted to tile
+// z-range [tz0, tz1).
+template <class F>
+__device__ __forceinline__ void for_each_tile(Grid g, Tiles t, int x, int y, int z, uint32_t R,
+                                              int tz0, int tz1, F f) {
+    const int r = static_cast<int>(isqrt_u32(R));
+    const int ax = max(x - r, 0) / kTile, bx = min(x + r, g.SX - 1) / kTile;
+    const int ay = max(y - r, 0) / kTile, by = min(y + r, g.SY - 1) / kTile;
+    const int az = max(max(z - r, 0) / kTile, tz0), bz = min(min(z + r, g.SZ - 1) / kTile, tz1 - 1);
+    for (int tz = az; tz <= bz; ++tz) {
+        const int lz = tz * kTile, hz = lz + kTile - 1;
+        const int dz = z < lz ? lz - z : (z > hz ? z - hz : 0);
+        for (int tx = ax; tx <= bx; ++tx) {
+            const int lx = tx * kTile, hx = lx + kTile - 1;
+            const int dx = x < lx ? lx - x : (x > hx ? x - hx : 0);
+            const int dxz = dx * dx + dz * dz;
+            if (static_cast<uint32_t>(dxz) > R) continue;
+            for (int ty = ay; ty <= by; ++ty) {
+                const int ly = ty * kTile, hy = ly + kTile - 1;
+                const int dy = y < ly ? ly - y : (y > hy ? y - hy : 0);
+                if (static_cast<uint32_t>(dxz + dy * dy) <= R) f(t.id(tx, ty, tz));
             }
         }
     }
 }
 
-__global__ void balls_unpack(const unsigned long long* __restrict__ keys, Geo g, size_t n,
+struct CountTile {
+    unsigned int* tcount;
+    __device__ void operator()(size_t tid) const { atomicAdd(&tcount[tid], 1u); }
+};
+
+struct FillTile {
+    const unsigned long long* toff;
+    unsigned long long base;
+    unsigned int* tcursor;
+    unsigned long long* entries;
+    unsigned long long key;
+    __device__ void operator()(size_t tid) const {
+        const unsigned pos = atomicAdd(&tcursor[tid], 1u);
+        entries[toff[tid] - base + pos] = key;
+    }
+};
+
+__global__ void balls_tile_count(const uint32_t* __restrict__ edt2, const uint32_t* __restrict__ cand,
+                                 size_t nc, Grid g, Tiles t, unsigned int* __restrict__ tcount) {
+    PMA_GRID_STRIDE(i, nc) {
+        const uint32_t v = cand[i];
+        int x, y, z;
+        g.coords(v, x, y, z);
+        for_each_tile(g, t, x, y, z, edt2[v], 0, t.TZ, CountTile{tcount});
+    }
+}
+
+__global__ void balls_tile_fill(const uint32_t* __restrict__ edt2, const uint32_t* __restrict__ cand,
+                                size_t nc, Grid g, Tiles t, int tz0, int tz1,
+                                const unsigned long long* __restrict__ toff, unsigned long long base,
+                                unsigned int* __restrict__ tcursor, unsigned long long* __restrict__ entries) {
+    PMA_GRID_STRIDE(i, nc) {
+        const uint32_t v = cand[i];
+        int x, y, z;
+        g.coords(v, x, y, z);
+        const uint32_t R = edt2[v];
+        const uint32_t lex = (static_cast<uint32_t>(x) * g.SY + y) * static_cast<uint32_t>(g.SZ) + z;
+        const unsigned long long key = (static_cast<unsigned long long>(R) << 32) | (0xFFFFFFFFu - lex);
+        for_each_tile(g, t, x, y, z, R, tz0, tz1, FillTile{toff, base, tcursor, entries, key});
+    }
+}
+
+__device__ __forceinline__ int4 decode_key(unsigned long long key, Grid g) {
+    const uint32_t lex = 0xFFFFFFFFu - static_cast<uint32_t>(key);
+    const uint32_t syz = static_cast<uint32_t>(g.SY) * g.SZ;
+    const uint32_t x = lex / syz, rem = lex % syz;
+    return make_int4(static_cast<int>(x), static_cast<int>(rem / g.SZ), static_cast<int>(rem % g.SZ),
+                     static_cast<int>(key >> 32));
+}
+
+__device__ __forceinline__ bool covers(int4 c, int vx, int vy, int vz) {
+    const long long dx = vx - c.x, dy = vy - c.y, dz = vz - c.z;
+    return dx * dx + dy * dy + dz * dz <= static_cast<long long>(static_cast<uint32_t>(c.w));
+}
+
+// One CTA per tile of the z-range starting at tz0: winner key of each voxel.
+__global__ void __launch_bounds__(kTileVox) balls_tile_gather(
+    const uint32_t* __restrict__ edt2, Grid g, Tiles t, int tz0,
+    const unsigned int* __restrict__ tcount, const unsigned long long* __restrict__ toff,
+    unsigned long long base, const unsigned long long* __restrict__ entries,
+    unsigned long long* __restrict__ keys, unsigned int* __restrict__ err) {
+    __shared__ unsigned long long s_key[kListCap];
+    __shared__ int4 s_pos[kListCap];
+    const size_t tile = static_cast<size_t>(tz0) * t.TX * t.TY + blockIdx.x;
+    const int ty = static_cast<int>(tile % t.TY);
+    const size_t rest = tile / t.TY;
+    const int tx = static_cast<int>(rest % t.TX);
+    const int tz = static_cast<int>(rest / t.TX);
+    // voxel of this thread: y fastest, then x, then z (a warp covers a 4 x 8 patch)
+    const int vy = ty * kTile + (threadIdx.x & 7);
+    const int vx = tx * kTile + ((threadIdx.x >> 3) & 7);
+    const int vz = tz * kTile + (threadIdx.x >> 6);
+    const bool inside = vx < g.SX && vy < g.SY && vz < g.SZ;
+    const size_t v = inside ? g.idx(vx, vy, vz) : 0;
+    const bool void_voxel = inside && edt2[v] != 0;
+    const unsigned int L = tcount[tile];
+    const unsigned long long* list = entries + (toff[tile] - base);
+    unsigned long long best = 0;
+    if (L <= static_cast<unsigned int>(kListCap)) {
+        unsigned int N = 1;
+        while (N < L) N <<= 1;
+        for (unsigned int i = threadIdx.x; i < N; i += blockDim.x) s_key[i] = (i < L) ? list[i] : 0ull;
+        __syncthreads();
+        // bitonic sort, descending
+        for (unsigned int k = 2; k <= N; k <<= 1) {
+            for (unsigned int j = k >> 1; j > 0; j >>= 1) {
+                for (unsigned int i = threadIdx.x; i < N; i += blockDim.x) {
+                    const unsigned int p = i ^ j;
+                    if (p > i) {
+                        const unsigned long long a = s_key[i], b = s_key[p];
+                        const bool desc = (i & k) == 0;
+                        if (desc ? (a < b) : (a > b)) {
+                            s_key[i] = b;
+                            s_key[p] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (unsigned int i = threadIdx.x; i < L; i += blockDim.x) s_pos[i] = decode_key(s_key[i], g);
+        __syncthreads();
+        if (void_voxel) {
+            for (unsigned int i = 0; i < L; ++i) {
+                if (covers(s_pos[i], vx, vy, vz)) {
+                    best = s_key[i];
+                    break;
+                }
+            }
+        }
+    } else {
+        // long list: unsorted chunks, keep the largest covering key
+        for (unsigned int c0 = 0; c0 < L; c0 += kListCap) {
+            const unsigned int m = min(static_cast<unsigned int>(kListCap), L - c0);
+            __syncthreads();
+            for (unsigned int i = threadIdx.x; i < m; i += blockDim.x) {
+                s_key[i] = list[c0 + i];
+                s_pos[i] = decode_key(s_key[i], g);
+            }
+            __syncthreads();
+            if (void_voxel) {
+                for (unsigned int i = 0; i < m; ++i)
+                    if (s_key[i] > best && covers(s_pos[i], vx, vy, vz)) best = s_key[i];
+            }
+        }
+    }
+    if (inside) {
+        if (void_voxel && best == 0) atomicOr(err, 2u);  // no kept ball covers a void voxel
+        keys[v] = void_voxel ? best : ~0ull;
+    }
+}
+
+__global__ void balls_unpack(const unsigned long long* __restrict__ keys, Grid g, size_t n,
                              uint32_t* __restrict__ crad2, uint32_t* __restrict__ cxo,
                              uint32_t* __restrict__ cyo, uint32_t* __restrict__ czo,
-                             uint8_t* __restrict__ mask, unsigned int* __restrict__ err) {
+                             uint8_t* __restrict__ mask) {
     const uint32_t syz = static_cast<uint32_t>(g.SY) * g.SZ;
-    for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
-         v += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    PMA_GRID_STRIDE(v, n) {
         const unsigned long long k = keys[v];
-        if (k == 0) atomicOr(err, 2u);  // a void voxel no kept ball covers: internal error
         if (k == ~0ull || k == 0) {
             crad2[v] = 0;
             cxo[v] = 0xFFFFFFFFu;
@@ -224,14 +306,12 @@ __global__ void balls_unpack(const unsigned long long* __restrict__ keys, Geo g,
     }
 }
 
-// Marks winning centres (OUTER = 255). Reads the packed keys rather than the three
-// coordinate arrays.
-__global__ void balls_mark(const unsigned long long* __restrict__ keys, Geo g, size_t n,
+// Marks winning centres (OUTER = 255) from the packed keys.
+__global__ void balls_mark(const unsigned long long* __restrict__ keys, Grid g, size_t n,
                            uint8_t* __restrict__ mask) {
-    const uint32_t limit = static_cast<uint32_t>(n);
     const uint32_t syz = static_cast<uint32_t>(g.SY) * g.SZ;
-    for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
-         v += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const uint32_t limit = static_cast<uint32_t>(n);
+    PMA_GRID_STRIDE(v, n) {
         const unsigned long long k = keys[v];
         if (k == ~0ull || k == 0) continue;
         const uint32_t lex = 0xFFFFFFFFu - static_cast<uint32_t>(k);
@@ -244,11 +324,14 @@ __global__ void balls_mark(const unsigned long long* __restrict__ keys, Geo g, s
 __global__ void count_value(const uint8_t* __restrict__ a, size_t n, uint8_t value,
                             unsigned long long* __restrict__ out) {
     unsigned long long c = 0;
-    for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
-         v += static_cast<size_t>(gridDim.x) * blockDim.x)
-        c += (a[v] == value);
+    PMA_GRID_STRIDE(v, n) c += (a[v] == value);
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+template <class T>
+T* buf(pma_ctx* ctx, const char* tag, size_t count) {
+    return static_cast<T*>(ctx->scratch(tag, std::max<size_t>(count, 1) * sizeof(T)));
 }
 
 }  // namespace
@@ -261,57 +344,93 @@ void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t m
                 "pma_containing_balls: null device pointer");
     cudaStream_t s = ctx->stream;
     const size_t n = voxels(d);
-    const Geo g{d.sx, d.sy, d.sz};
+    const Grid g{d.sx, d.sy, d.sz};
     const uint32_t nR = max_edt2 + 1;
     const uint32_t ntab = std::min<uint32_t>(nR, kExactTable);
-    const unsigned grid = static_cast<unsigned>(std::min<size_t>(div_up(n, 256), ctx->num_sms * 16ull));
+    const unsigned G = grid_for(ctx, n);
 
-    auto* keys = static_cast<unsigned long long*>(ctx->scratch("balls.keys", n * 8));
-    auto* mtab = static_cast<uint32_t*>(ctx->scratch("balls.mtab", 3ull * ntab * 4));
-    auto* counts = static_cast<uint32_t*>(ctx->scratch("balls.counts", (2ull * nR + 6) * 4));
-    uint32_t* cursor = counts + nR;
-    uint32_t* misc = cursor + nR;  // [0] total, [1] next, [2..3] count, [4] error flags
-    auto* list = static_cast<uint32_t*>(ctx->scratch("balls.list", n * 4));
+    auto* keys = buf<unsigned long long>(ctx, "balls.keys", n);
+    auto* mtab = buf<uint32_t>(ctx, "balls.mtab", 3ull * ntab);
+    auto* misc = buf<unsigned long long>(ctx, "balls.misc", 4);  // [0] count, [1] err, [2] select
+    auto* err = reinterpret_cast<unsigned int*>(misc + 1);
+    PMA_CUDA(cudaMemsetAsync(misc, 0, 32, s));
 
+    // Kept centres.
     balls_containment_table<<<div_up(ntab, 128), 128, 0, s>>>(mtab, mtab + ntab, mtab + 2 * ntab, ntab);
     ctx->check_launch("balls_containment_table");
-    PMA_CUDA(cudaMemsetAsync(counts, 0, (2ull * nR + 6) * 4, s));
-    unsigned int* err = misc + 4;
+    uint8_t* flags = buf<uint8_t>(ctx, "balls.flags", n);
+    uint32_t* cand = buf<uint32_t>(ctx, "balls.cand", n);
+    int64_t nc = 0;
     {
-    KernelTimer kt(ctx, "balls_candidates");
-    balls_candidates<false><<<grid, 256, 0, s>>>(edt2, g, n, mtab, ntab, nR, counts, nullptr, nullptr,
-                                                 keys, err);
-    ctx->check_launch("balls_candidates(count)");
-    balls_bucket_offsets<<<1, 1024, 0, s>>>(counts, cursor, nR, misc);
-    ctx->check_launch("balls_bucket_offsets");
-    balls_candidates<true><<<grid, 256, 0, s>>>(edt2, g, n, mtab, ntab, nR, counts, cursor, list,
-                                                keys, err);
-    ctx->check_launch("balls_candidates(place)");
+        KernelTimer kt(ctx, "balls_candidates");
+        balls_candidate_flags<<<G, 256, 0, s>>>(edt2, g, n, mtab, ntab, nR, flags, err);
+        ctx->check_launch("balls_candidate_flags");
+        nc = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), flags, cand,
+                            static_cast<int64_t>(n), reinterpret_cast<int64_t*>(misc + 2));
     }
-    uint32_t hm[5] = {0, 0, 0, 0, 0};
-    PMA_CUDA(cudaMemcpyAsync(hm, misc, sizeof(hm), cudaMemcpyDeviceToHost, s));
+    unsigned int h_err = 0;
+    PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
     ctx->sync();
-    PMA_REQUIRE(!(hm[4] & 1u), PMA_ERR_ARGUMENT,
+    PMA_REQUIRE(!(h_err & 1u), PMA_ERR_ARGUMENT,
                 "pma_containing_balls: max_edt2 is smaller than the largest squared distance");
-    const uint32_t total = hm[0];
-    if (total) {
-        KernelTimer kt(ctx, "balls_scatter");
-        balls_scatter<<<ctx->num_sms * 8, 256, 0, s>>>(edt2, g, list, total, misc + 1, keys);
-        ctx->check_launch("balls_scatter");
+
+    // Tile lists: counts, 64-bit offsets (host scan), then fill + gather by tile z-ranges
+    // whose entries fit the memory budget.
+    Tiles t{(d.sx + kTile - 1) / kTile, (d.sy + kTile - 1) / kTile, (d.sz + kTile - 1) / kTile};
+    const size_t per_z = static_cast<size_t>(t.TX) * t.TY;
+    const size_t ntiles = per_z * t.TZ;
+    unsigned int* tcount = buf<unsigned int>(ctx, "balls.tcount", ntiles);
+    unsigned int* tcursor = buf<unsigned int>(ctx, "balls.tcursor", ntiles);
+    auto* toff = buf<unsigned long long>(ctx, "balls.toff", ntiles + 1);
+    PMA_CUDA(cudaMemsetAsync(tcount, 0, ntiles * 4, s));
+    PMA_CUDA(cudaMemsetAsync(tcursor, 0, ntiles * 4, s));
+    if (nc) {
+        KernelTimer kt(ctx, "balls_tile_count");
+        balls_tile_count<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, tcount);
+        ctx->check_launch("balls_tile_count");
     }
-    balls_unpack<<<grid, 256, 0, s>>>(keys, g, n, crad2, cx, cy, cz, mask, err);
+    std::vector<unsigned int> hc(ntiles);
+    PMA_CUDA(cudaMemcpyAsync(hc.data(), tcount, ntiles * 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    std::vector<unsigned long long> ho(ntiles + 1, 0);
+    for (size_t i = 0; i < ntiles; ++i) ho[i + 1] = ho[i] + hc[i];
+    PMA_CUDA(cudaMemcpyAsync(toff, ho.data(), (ntiles + 1) * 8, cudaMemcpyHostToDevice, s));
+    size_t free_b = 0, total_b = 0;
+    PMA_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const unsigned long long budget = std::max<unsigned long long>(
+        1ull << 20, std::min<unsigned long long>(free_b / 3, 32ull << 30) / 8);
+    for (int z0 = 0; z0 < t.TZ;) {
+        int z1 = z0 + 1;
+        while (z1 < t.TZ && ho[(z1 + 1) * per_z] - ho[z0 * per_z] <= budget) ++z1;
+        const unsigned long long base = ho[z0 * per_z];
+        const unsigned long long cnt = ho[z1 * per_z] - base;
+        auto* entries = buf<unsigned long long>(ctx, "balls.entries", cnt);
+        if (nc) {
+            KernelTimer kt(ctx, "balls_tile_fill");
+            balls_tile_fill<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, z0, z1, toff, base,
+                                                              tcursor, entries);
+            ctx->check_launch("balls_tile_fill");
+        }
+        {
+            KernelTimer kt(ctx, "balls_tile_gather");
+            balls_tile_gather<<<static_cast<unsigned>((z1 - z0) * per_z), kTileVox, 0, s>>>(
+                edt2, g, t, z0, tcount, toff, base, entries, keys, err);
+            ctx->check_launch("balls_tile_gather");
+        }
+        z0 = z1;
+    }
+    balls_unpack<<<G, 256, 0, s>>>(keys, g, n, crad2, cx, cy, cz, mask);
     ctx->check_launch("balls_unpack");
-    balls_mark<<<grid, 256, 0, s>>>(keys, g, n, mask);
+    balls_mark<<<G, 256, 0, s>>>(keys, g, n, mask);
     ctx->check_launch("balls_mark");
-    auto* d_count = reinterpret_cast<unsigned long long*>(misc + 2);
-    PMA_CUDA(cudaMemsetAsync(d_count, 0, 8, s));
-    count_value<<<grid, 256, 0, s>>>(mask, n, 255, d_count);
+    PMA_CUDA(cudaMemsetAsync(misc, 0, 8, s));
+    count_value<<<G, 256, 0, s>>>(mask, n, 255, misc);
     ctx->check_launch("count_value");
     unsigned long long c = 0;
-    PMA_CUDA(cudaMemcpyAsync(&c, d_count, 8, cudaMemcpyDeviceToHost, s));
-    PMA_CUDA(cudaMemcpyAsync(hm, misc, sizeof(hm), cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(&c, misc, 8, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
     ctx->sync();
-    PMA_REQUIRE(!(hm[4] & 2u), PMA_ERR_INTERNAL, "pma_containing_balls: uncovered void voxel");
+    PMA_REQUIRE(!(h_err & 2u), PMA_ERR_INTERNAL, "pma_containing_balls: uncovered void voxel");
     if (count) *count = c;
 }
 
