@@ -39,6 +39,19 @@ __device__ __forceinline__ bool stencil_offset(int j, bool d3q7, int& dx, int& d
     return true;
 }
 
+// Two independent 64-bit hashes of an id sequence (FNV-1a and a multiply-xorshift stream).
+// Sets are compared by both hashes and then verified element by element.
+__device__ __forceinline__ void list_hash(const uint32_t* a, uint32_t n, unsigned long long& h1,
+                                          unsigned long long& h2) {
+    h1 = 1469598103934665603ull ^ n;
+    h2 = 0x9E3779B97F4A7C15ull + n;
+    for (uint32_t i = 0; i < n; ++i) {
+        h1 = (h1 ^ a[i]) * 1099511628211ull;
+        h2 = (h2 + a[i] + 0x632BE59BD9B4E019ull) * 0xD6E8FEB86659FD93ull;
+        h2 ^= h2 >> 32;
+    }
+}
+
 // --- CUB wrappers (all on ctx->stream; temporary storage cached in the context) ----------
 
 template <class InIt, class T>

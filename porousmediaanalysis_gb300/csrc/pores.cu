@@ -318,18 +318,6 @@ __global__ void level_advance(unsigned long long* __restrict__ base, const unsig
     if (threadIdx.x == 0 && blockIdx.x == 0) *base += off[nlev - 1] + cnt[nlev - 1];
 }
 
-// FNV-1a style 64-bit hashes of a sorted rank list (two independent streams).
-__device__ __forceinline__ void list_hash(const uint32_t* a, uint32_t n, unsigned long long& h1,
-                                          unsigned long long& h2) {
-    h1 = 1469598103934665603ull ^ n;
-    h2 = 0x9E3779B97F4A7C15ull + n;
-    for (uint32_t i = 0; i < n; ++i) {
-        h1 = (h1 ^ a[i]) * 1099511628211ull;
-        h2 = (h2 + a[i] + 0x632BE59BD9B4E019ull) * 0xD6E8FEB86659FD93ull;
-        h2 ^= h2 >> 32;
-    }
-}
-
 __global__ void throat_hashes(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
                               const uint32_t* __restrict__ pool, const uint32_t* __restrict__ multi,
                               size_t nm, unsigned long long* __restrict__ h1o,

@@ -10,22 +10,25 @@
 // Parallel replay. Within one depth the FIFO runs generation by generation: generation 0 is
 // the queue content when the depth starts (seeds in pore-id order, then nodes queued while
 // deeper levels ran, in queue order); generation k+1 is what generation k queues at the same
-// depth, in push order. Every touch gets the time (generation, position of its node in the
-// generation * 27 + neighbour index), which orders touches exactly as the sequential loop
-// does. Per generation:
+// depth, in push order. Every touch gets the time (generation, node position * 27 +
+// neighbour index), which orders touches exactly as the sequential loop does. Per generation:
 //   claim    - the smallest-time touch of each unclaimed voxel wins (atomicMin on time);
-//   extend   - touches by other pores record, per voxel and pore, their first touch time;
-//   queue    - claimed voxels in time order form the next generation (same depth) or are
-//              appended, time-stamped, to the bucket of their depth, which is sorted by time
-//              when that depth starts.
-// Shared types are created at their first extension time, so sorting keys by that time
-// reproduces the reference's id sequence (UINT32_MAX - 1, - 2, ...) exactly, including types
-// whose volume later drops to zero.
+//   resolve  - the winner records the claim; a voxel of the same depth joins the next
+//              generation, a shallower one is appended, time-stamped, to its depth's bucket,
+//              which is sorted by time when that depth starts;
+//   extend   - touches by other pores record, per voxel and pore, their first touch time.
+// Frontier sizes stay on the device; the next generation is compacted in event order by a
+// count / scan / scatter over event slots stamped with the generation number.
+//
+// Shared types: a voxel's key is its claimer plus its extending pores in time order; every
+// prefix of length >= 2 was created at the time of its last extension. All prefixes are
+// hashed, grouped with radix sorts and ranked by creation time on the device, which
+// reproduces the reference's id sequence (UINT32_MAX - 1, - 2, ...) exactly, including
+// types whose volume later dropped to zero.
 #include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
 #include <cstring>
-#include <map>
 #include <vector>
 
 #include "devutil.cuh"
@@ -35,21 +38,30 @@ namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kNoTime = ~0ull;
-constexpr int kSlots = 6;  // distinct extending pores recorded per shared voxel
+constexpr int kSlots = 6;         // distinct extending pores recorded per shared voxel
+constexpr int kKey = kSlots + 1;  // longest key
+constexpr int kChunk = 1024;      // event slots per compaction block
+constexpr int kGensPerSync = 8;
 
 struct WsState {
     Grid g;
     int d3q7;
     const uint32_t* crad;
-    uint32_t* claim;             // pore index + 1, 0 = unclaimed
-    unsigned long long* ckey;    // per-generation claim time (kNoTime when idle)
-    uint32_t* ext;               // shared-voxel record + 1, 0 = none
-    uint32_t* ext_pore;          // [records][kSlots]
+    uint32_t* claim;              // pore index + 1, 0 = unclaimed
+    unsigned long long* ckey;     // per-generation claim time (kNoTime when idle)
+    uint32_t* ext;                // shared-voxel record + 1, 0 = none
+    uint32_t* ext_pore;           // [records][kSlots]
     unsigned long long* ext_time;
     unsigned int* ext_count;
     uint32_t ext_cap;
-    unsigned int* pbound;        // per pore
+    unsigned int* pbound;         // per pore
     unsigned int* err;
+    uint32_t* slot_gen;           // generation stamp of same-depth claims, per event slot
+    uint32_t* slot_voxel;
+    const unsigned long long* boff;  // bucket offsets
+    unsigned int* bfill;
+    unsigned long long* ent_time;
+    unsigned long long* ent_val;
 };
 
 __global__ void ws_init(size_t n, uint32_t* __restrict__ claim, unsigned long long* __restrict__ ckey,
@@ -65,12 +77,27 @@ __global__ void ws_seed(const uint32_t* __restrict__ seed_voxel, size_t np, uint
     PMA_GRID_STRIDE(k, np) claim[seed_voxel[k]] = static_cast<uint32_t>(k + 1);
 }
 
-// Touch events of generation nodes: claims (phase 0), claim resolution (phase 1),
-// extensions (phase 2). Node i, neighbour j has event number i * 27 + j.
+__global__ void ws_seed_entries(const unsigned long long* __restrict__ a, size_t np,
+                                unsigned long long* __restrict__ ent_time,
+                                unsigned long long* __restrict__ ent_val) {
+    PMA_GRID_STRIDE(k, np) {
+        ent_time[a[k]] = a[np + k];
+        ent_val[a[k]] = a[2 * np + k];
+    }
+}
+
+__global__ void ws_histograms(const uint32_t* __restrict__ crad, size_t n, unsigned int* __restrict__ hist) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t r = crad[v];
+        if (r) atomicAdd(&hist[r], 1u);
+    }
+}
+
+// Touch events of the generation's nodes. Phase 0 claims, 1 resolves, 2 extends.
 template <int kPhase>
 __global__ void ws_touch(WsState s, const uint32_t* __restrict__ gv, const uint32_t* __restrict__ gp,
-                         size_t ng, uint32_t depth, unsigned long long gen,
-                         uint32_t* __restrict__ slot_voxel) {
+                         const unsigned int* __restrict__ d_ng, uint32_t depth, unsigned long long gen) {
+    const size_t ng = *d_ng;
     PMA_GRID_STRIDE(i, ng) {
         const uint32_t v = gv[i];
         const uint32_t pore = gp[i];
@@ -91,14 +118,20 @@ __global__ void ws_touch(WsState s, const uint32_t* __restrict__ gv, const uint3
             if (kPhase == 0) {
                 if (s.claim[w] == 0) atomicMin(&s.ckey[w], seq);
             } else if (kPhase == 1) {
-                if (s.ckey[w] == seq) {
-                    s.claim[w] = pore + 1;
-                    s.ckey[w] = kNoTime;
-                    slot_voxel[seq] = static_cast<uint32_t>(w);
+                if (s.ckey[w] != seq) continue;
+                s.claim[w] = pore + 1;
+                s.ckey[w] = kNoTime;
+                if (r == depth) {
+                    s.slot_voxel[seq] = static_cast<uint32_t>(w);
+                    s.slot_gen[seq] = static_cast<uint32_t>(gen);
+                } else {
+                    const unsigned pos = atomicAdd(&s.bfill[r], 1u);
+                    const unsigned long long at = s.boff[r] + pos;
+                    s.ent_time[at] = (gen << 40) | seq;
+                    s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
                 }
             } else {
                 if (s.claim[w] == pore + 1) continue;
-                // record (pore, first touch time) for w
                 uint32_t rec = s.ext[w];
                 if (rec == 0) {
                     const uint32_t fresh = atomicAdd(s.ext_count, 1u) + 1;
@@ -125,44 +158,111 @@ __global__ void ws_touch(WsState s, const uint32_t* __restrict__ gv, const uint3
     }
 }
 
-struct SlotTaken {
-    const uint32_t* slot_voxel;
-    __host__ __device__ bool operator()(uint32_t seq) const { return slot_voxel[seq] != kNone; }
-};
-
-struct AtDepth {
-    const uint32_t* slot_voxel;
-    const uint32_t* crad;
-    uint32_t depth;
-    __host__ __device__ bool operator()(uint32_t seq) const { return crad[slot_voxel[seq]] == depth; }
-};
-
-// Claimed voxels in event order: same depth -> next generation, deeper -> their bucket.
-__global__ void ws_distribute(const uint32_t* __restrict__ claimed, size_t nc,
-                              const uint32_t* __restrict__ slot_voxel, const uint32_t* __restrict__ gp,
-                              const uint32_t* __restrict__ crad, uint32_t depth, unsigned long long gen,
-                              const unsigned long long* __restrict__ boff, unsigned int* __restrict__ bfill,
-                              unsigned long long* __restrict__ ent_time,
-                              unsigned long long* __restrict__ ent_val) {
-    PMA_GRID_STRIDE(r, nc) {
-        const uint32_t seq = claimed[r];
-        const uint32_t w = slot_voxel[seq];
-        const uint32_t b = crad[w];
-        if (b == depth) continue;
-        const unsigned pos = atomicAdd(&bfill[b], 1u);
-        const unsigned long long at = boff[b] + pos;
-        ent_time[at] = (gen << 40) | r;
-        ent_val[at] = (static_cast<unsigned long long>(gp[seq / 27]) << 32) | w;
+// Ordered compaction of this generation's same-depth claims: counts per chunk of event slots.
+__global__ void ws_slot_count(const uint32_t* __restrict__ slot_gen, const unsigned int* __restrict__ d_ng,
+                              uint32_t gen, unsigned int* __restrict__ ccount) {
+    const size_t nev = static_cast<size_t>(*d_ng) * 27;
+    const size_t nchunks = (nev + kChunk - 1) / kChunk;
+    __shared__ unsigned int part[32];
+    for (size_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        unsigned int local = 0;
+        for (size_t k = threadIdx.x; k < kChunk; k += blockDim.x) {
+            const size_t e = c * kChunk + k;
+            local += (e < nev && slot_gen[e] == gen) ? 1u : 0u;
+        }
+        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = local;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int sum = 0;
+            for (unsigned w = 0; w < (blockDim.x + 31) / 32; ++w) sum += part[w];
+            ccount[c] = sum;
+        }
+        __syncthreads();
     }
 }
 
-__global__ void ws_next_generation(const uint32_t* __restrict__ sel, size_t n,
-                                   const uint32_t* __restrict__ slot_voxel, const uint32_t* __restrict__ gp,
-                                   uint32_t* __restrict__ nv, uint32_t* __restrict__ np_) {
-    PMA_GRID_STRIDE(i, n) {
-        const uint32_t seq = sel[i];
-        nv[i] = slot_voxel[seq];
-        np_[i] = gp[seq / 27];
+// Exclusive scan of chunk counts (one block); writes the next generation's size.
+__global__ void ws_slot_scan(unsigned int* __restrict__ ccount, const unsigned int* __restrict__ d_ng,
+                             unsigned int* __restrict__ d_ng_next) {
+    const size_t nev = static_cast<size_t>(*d_ng) * 27;
+    const size_t nchunks = (nev + kChunk - 1) / kChunk;
+    __shared__ unsigned int part[1024];
+    const size_t per = (nchunks + blockDim.x - 1) / blockDim.x;
+    unsigned int s = 0;
+    for (size_t k = 0; k < per; ++k) {
+        const size_t c = threadIdx.x * per + k;
+        if (c < nchunks) s += ccount[c];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int run = 0;
+        for (unsigned t = 0; t < blockDim.x; ++t) {
+            const unsigned int v = part[t];
+            part[t] = run;
+            run += v;
+        }
+        *d_ng_next = run;
+    }
+    __syncthreads();
+    unsigned int run = part[threadIdx.x];
+    for (size_t k = 0; k < per; ++k) {
+        const size_t c = threadIdx.x * per + k;
+        if (c < nchunks) {
+            const unsigned int v = ccount[c];
+            ccount[c] = run;
+            run += v;
+        }
+    }
+}
+
+// Writes the same-depth claims in event order as the next generation (voxel, pore).
+// blockDim.x == kChunk / 4: each thread owns 4 consecutive slots of the block's chunk.
+__global__ void ws_slot_scatter(const uint32_t* __restrict__ slot_gen, const uint32_t* __restrict__ slot_voxel,
+                                const unsigned int* __restrict__ d_ng, uint32_t gen,
+                                const unsigned int* __restrict__ coff, const uint32_t* __restrict__ gp,
+                                uint32_t* __restrict__ nv, uint32_t* __restrict__ np_) {
+    const size_t nev = static_cast<size_t>(*d_ng) * 27;
+    const size_t nchunks = (nev + kChunk - 1) / kChunk;
+    __shared__ unsigned int warp_sum[32];
+    for (size_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const unsigned int base = coff[c];
+        const size_t e0 = c * kChunk + static_cast<size_t>(threadIdx.x) * 4;
+        unsigned int f[4];
+        unsigned int mine = 0;
+        for (int k = 0; k < 4; ++k) {
+            const size_t e = e0 + k;
+            f[k] = (e < nev && slot_gen[e] == gen) ? 1u : 0u;
+            mine += f[k];
+        }
+        const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        unsigned int incl = mine;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<unsigned>(o)) incl += t;
+        }
+        if (lane == 31) warp_sum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const unsigned nw = (blockDim.x + 31) / 32;
+            unsigned int wsum = lane < nw ? warp_sum[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int t = __shfl_up_sync(0xFFFFFFFFu, wsum, o);
+                if (lane >= static_cast<unsigned>(o)) wsum += t;
+            }
+            if (lane < nw) warp_sum[lane] = wsum;  // inclusive over warps
+        }
+        __syncthreads();
+        unsigned int pos = base + (warp ? warp_sum[warp - 1] : 0u) + incl - mine;
+        for (int k = 0; k < 4; ++k) {
+            if (!f[k]) continue;
+            const size_t e = e0 + k;
+            nv[pos] = slot_voxel[e];
+            np_[pos] = gp[e / 27];
+            ++pos;
+        }
+        __syncthreads();
     }
 }
 
@@ -171,22 +271,6 @@ __global__ void ws_unpack_entries(const unsigned long long* __restrict__ val, si
     PMA_GRID_STRIDE(i, n) {
         gv[i] = static_cast<uint32_t>(val[i]);
         gp[i] = static_cast<uint32_t>(val[i] >> 32);
-    }
-}
-
-__global__ void ws_seed_entries(const unsigned long long* __restrict__ a, size_t np,
-                                unsigned long long* __restrict__ ent_time,
-                                unsigned long long* __restrict__ ent_val) {
-    PMA_GRID_STRIDE(k, np) {
-        ent_time[a[k]] = a[np + k];
-        ent_val[a[k]] = a[2 * np + k];
-    }
-}
-
-__global__ void ws_histograms(const uint32_t* __restrict__ crad, size_t n, unsigned int* __restrict__ hist) {
-    PMA_GRID_STRIDE(v, n) {
-        const uint32_t r = crad[v];
-        if (r) atomicAdd(&hist[r], 1u);
     }
 }
 
@@ -200,18 +284,104 @@ __global__ void ws_volumes(const uint32_t* __restrict__ claim, const uint32_t* _
     }
 }
 
-__global__ void ws_gather_shared(const uint32_t* __restrict__ sv, size_t ns, const uint32_t* __restrict__ claim,
-                                 const uint32_t* __restrict__ ext, const uint32_t* __restrict__ ext_pore,
-                                 const unsigned long long* __restrict__ ext_time, uint32_t* __restrict__ oc,
-                                 uint32_t* __restrict__ op, unsigned long long* __restrict__ ot) {
+// --- shared types -------------------------------------------------------------------------
+
+// Key of shared voxel i: [first extension, claimer, later extensions...] in pore indices,
+// and one record per prefix of length L = 2..len (record i * kSlots + L - 2).
+__global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const uint32_t* __restrict__ claim,
+                        const uint32_t* __restrict__ ext, const uint32_t* __restrict__ ext_pore,
+                        const unsigned long long* __restrict__ ext_time, uint32_t* __restrict__ kseq,
+                        uint8_t* __restrict__ klen, unsigned long long* __restrict__ rh1,
+                        unsigned long long* __restrict__ rh2, unsigned long long* __restrict__ rtime,
+                        uint8_t* __restrict__ rvalid) {
     PMA_GRID_STRIDE(i, ns) {
         const uint32_t v = sv[i];
-        oc[i] = claim[v];
         const uint32_t rec = ext[v] - 1;
+        uint32_t p[kSlots];
+        unsigned long long t[kSlots];
+        int m = 0;
         for (int k = 0; k < kSlots; ++k) {
-            op[i * kSlots + k] = ext_pore[static_cast<size_t>(rec) * kSlots + k];
-            ot[i * kSlots + k] = ext_time[static_cast<size_t>(rec) * kSlots + k];
+            const uint32_t pk = ext_pore[static_cast<size_t>(rec) * kSlots + k];
+            if (pk == kNone) continue;
+            p[m] = pk;
+            t[m] = ext_time[static_cast<size_t>(rec) * kSlots + k];
+            ++m;
         }
+        for (int a = 1; a < m; ++a)  // insertion sort by time
+            for (int b = a; b > 0 && t[b] < t[b - 1]; --b) {
+                const unsigned long long tt = t[b];
+                t[b] = t[b - 1];
+                t[b - 1] = tt;
+                const uint32_t pp = p[b];
+                p[b] = p[b - 1];
+                p[b - 1] = pp;
+            }
+        uint32_t key[kKey];
+        key[0] = p[0];
+        key[1] = claim[v] - 1;
+        for (int k = 1; k < m; ++k) key[k + 1] = p[k];
+        const int len = m + 1;
+        for (int k = 0; k < kKey; ++k) kseq[i * kKey + k] = k < len ? key[k] : kNone;
+        klen[i] = static_cast<uint8_t>(len);
+        for (int L = 2; L <= kKey; ++L) {
+            const size_t r = i * kSlots + (L - 2);
+            if (L <= len) {
+                unsigned long long a, b;
+                list_hash(key, static_cast<uint32_t>(L), a, b);
+                rh1[r] = a;
+                rh2[r] = b;
+                rtime[r] = t[L - 2];
+                rvalid[r] = 1;
+            } else {
+                rvalid[r] = 0;
+            }
+        }
+    }
+}
+
+__global__ void ws_gather_h(const unsigned long long* __restrict__ h, const uint32_t* __restrict__ idx,
+                            size_t n, unsigned long long* __restrict__ out) {
+    PMA_GRID_STRIDE(i, n) out[i] = h[idx[i]];
+}
+
+__global__ void ws_group_starts(const uint32_t* __restrict__ rec, size_t nr,
+                                const unsigned long long* __restrict__ rh1,
+                                const unsigned long long* __restrict__ rh2,
+                                const uint32_t* __restrict__ kseq, uint32_t* __restrict__ start,
+                                unsigned int* __restrict__ err) {
+    PMA_GRID_STRIDE(i, nr) {
+        const uint32_t r = rec[i];
+        bool s = i == 0;
+        if (!s) {
+            const uint32_t q = rec[i - 1];
+            s = rh1[r] != rh1[q] || rh2[r] != rh2[q];
+            if (!s) {  // verify: same prefix
+                const uint32_t L = r % kSlots + 2, Lq = q % kSlots + 2;
+                bool eq = L == Lq;
+                for (uint32_t k = 0; eq && k < L; ++k)
+                    eq = kseq[(r / kSlots) * kKey + k] == kseq[(q / kSlots) * kKey + k];
+                if (!eq) atomicOr(err, 4u);
+            }
+        }
+        start[i] = s ? 1u : 0u;
+    }
+}
+
+__global__ void ws_group_reduce(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ excl,
+                                const uint32_t* __restrict__ start, size_t nr,
+                                const unsigned long long* __restrict__ rtime, const uint8_t* __restrict__ klen,
+                                unsigned long long* __restrict__ gtime, unsigned long long* __restrict__ gvol,
+                                uint32_t* __restrict__ grep, uint32_t* __restrict__ final_group) {
+    PMA_GRID_STRIDE(i, nr) {
+        const uint32_t r = rec[i];
+        const uint32_t g = excl[i] + start[i] - 1u;
+        atomicMin(&gtime[g], rtime[r]);
+        const uint32_t vi = r / kSlots, L = r % kSlots + 2;
+        if (L == klen[vi]) {
+            atomicAdd(&gvol[g], 1ull);
+            final_group[vi] = g;
+        }
+        if (start[i]) grep[g] = r;
     }
 }
 
@@ -223,35 +393,23 @@ __global__ void ws_labels(const uint32_t* __restrict__ claim, size_t n, const ui
     }
 }
 
-__global__ void ws_shared_labels(const uint32_t* __restrict__ sv, const uint32_t* __restrict__ id, size_t ns,
-                                 uint32_t* __restrict__ labels) {
-    PMA_GRID_STRIDE(i, ns) labels[sv[i]] = id[i];
+__global__ void ws_shared_labels(const uint32_t* __restrict__ sv, const uint32_t* __restrict__ final_group,
+                                 const uint32_t* __restrict__ gid, size_t ns, uint32_t* __restrict__ labels) {
+    PMA_GRID_STRIDE(i, ns) labels[sv[i]] = gid[final_group[i]];
+}
+
+__global__ void ws_group_rows(const uint32_t* __restrict__ grep, size_t ngr, const uint32_t* __restrict__ kseq,
+                              uint32_t* __restrict__ out) {
+    PMA_GRID_STRIDE(g, ngr) {
+        const uint32_t r = grep[g];
+        const uint32_t L = r % kSlots + 2, vi = r / kSlots;
+        for (int k = 0; k < kKey; ++k) out[g * kKey + k] = k < static_cast<int>(L) ? kseq[vi * kKey + k] : kNone;
+    }
 }
 
 template <class T>
 T* buf(pma_ctx* ctx, const char* tag, size_t count) {
     return static_cast<T*>(ctx->scratch(tag, std::max<size_t>(count, 1) * sizeof(T)));
-}
-
-template <class Pred>
-int64_t select_seqs(pma_ctx* ctx, Pred pred, const uint32_t* in_or_null, uint32_t* out, int64_t n,
-                    int64_t* d_count) {
-    size_t bytes = 0;
-    if (in_or_null) {
-        PMA_CUDA(cub::DeviceSelect::If(nullptr, bytes, in_or_null, out, d_count, n, pred, ctx->stream));
-        void* tmp = ctx->scratch("cub.tmp", bytes);
-        PMA_CUDA(cub::DeviceSelect::If(tmp, bytes, in_or_null, out, d_count, n, pred, ctx->stream));
-    } else {
-        thrust::counting_iterator<uint32_t> it(0);
-        PMA_CUDA(cub::DeviceSelect::If(nullptr, bytes, it, out, d_count, n, pred, ctx->stream));
-        void* tmp = ctx->scratch("cub.tmp", bytes);
-        PMA_CUDA(cub::DeviceSelect::If(tmp, bytes, it, out, d_count, n, pred, ctx->stream));
-    }
-    int64_t h = 0;
-    PMA_CUDA(cudaMemcpyAsync(&h, d_count, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    ctx->sync();
-    ctx->count_launch(1);
-    return h;
 }
 
 }  // namespace
@@ -276,8 +434,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         const pma_pore& p = pores[k];
         PMA_REQUIRE(g.inside(p.seed_x, p.seed_y, p.seed_z), PMA_ERR_ARGUMENT,
                     "pma_watershed: pore seed outside the image");
-        PMA_REQUIRE(p.seed_r2 <= max_edt2, PMA_ERR_ARGUMENT,
-                    "pma_watershed: pore seed radius above max_edt2");
+        PMA_REQUIRE(p.seed_r2 <= max_edt2, PMA_ERR_ARGUMENT, "pma_watershed: pore seed radius above max_edt2");
         seed_voxel[k] = static_cast<uint32_t>(g.idx(p.seed_x, p.seed_y, p.seed_z));
         seed_hist[p.seed_r2]++;
     }
@@ -289,6 +446,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     }
 
     int64_t* d_count = buf<int64_t>(ctx, "ws.count", 4);
+    unsigned int* d_ng = reinterpret_cast<unsigned int*>(d_count + 3);  // two frontier sizes
     WsState ws;
     ws.g = g;
     ws.d3q7 = st == PMA_D3Q7 ? 1 : 0;
@@ -326,87 +484,81 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     }
     const unsigned long long total = boff[nb];
     auto* d_boff = buf<unsigned long long>(ctx, "ws.boff", nb + 1);
-    unsigned int* bfill = buf<unsigned int>(ctx, "ws.bfill", nb);
-    auto* ent_time = buf<unsigned long long>(ctx, "ws.ent_time", total);
-    auto* ent_val = buf<unsigned long long>(ctx, "ws.ent_val", total);
+    ws.boff = d_boff;
+    ws.bfill = buf<unsigned int>(ctx, "ws.bfill", nb);
+    ws.ent_time = buf<unsigned long long>(ctx, "ws.ent_time", total);
+    ws.ent_val = buf<unsigned long long>(ctx, "ws.ent_val", total);
     auto* srt_time = buf<unsigned long long>(ctx, "ws.srt_time", max_bucket);
     auto* srt_val = buf<unsigned long long>(ctx, "ws.srt_val", max_bucket);
+    const size_t max_events = max_bucket * 27;
+    ws.slot_gen = buf<uint32_t>(ctx, "ws.slot_gen", max_events);
+    ws.slot_voxel = buf<uint32_t>(ctx, "ws.slot_voxel", max_events);
+    PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));  // generations start at 1
+    unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", (max_events + kChunk - 1) / kChunk);
     PMA_CUDA(cudaMemcpyAsync(d_boff, boff.data(), (nb + 1) * 8ull, cudaMemcpyHostToDevice, s));
-    // Seeds first in their bucket, in pore-id order (time = pore index).
     std::vector<unsigned int> h_fill(nb, 0);
     if (npores) {
-        std::vector<unsigned long long> at(npores), tv(npores), vv(npores);
+        std::vector<unsigned long long> a(3 * npores);
         for (size_t k = 0; k < npores; ++k) {
             const uint32_t b = pores[k].seed_r2;
-            at[k] = boff[b] + h_fill[b]++;
-            tv[k] = k;
-            vv[k] = (static_cast<unsigned long long>(k) << 32) | seed_voxel[k];
+            a[k] = boff[b] + h_fill[b]++;
+            a[npores + k] = k;  // seeds come first in their bucket, in pore-id order
+            a[2 * npores + k] = (static_cast<unsigned long long>(k) << 32) | seed_voxel[k];
         }
-        auto* d_at = buf<unsigned long long>(ctx, "ws.seed_at", 3 * npores);
-        PMA_CUDA(cudaMemcpyAsync(d_at, at.data(), npores * 8, cudaMemcpyHostToDevice, s));
-        PMA_CUDA(cudaMemcpyAsync(d_at + npores, tv.data(), npores * 8, cudaMemcpyHostToDevice, s));
-        PMA_CUDA(cudaMemcpyAsync(d_at + 2 * npores, vv.data(), npores * 8, cudaMemcpyHostToDevice, s));
-        ws_seed_entries<<<grid_for(ctx, npores), 256, 0, s>>>(d_at, npores, ent_time, ent_val);
+        auto* d_a = buf<unsigned long long>(ctx, "ws.seed_at", 3 * npores);
+        PMA_CUDA(cudaMemcpyAsync(d_a, a.data(), 3 * npores * 8, cudaMemcpyHostToDevice, s));
+        ws_seed_entries<<<grid_for(ctx, npores), 256, 0, s>>>(d_a, npores, ws.ent_time, ws.ent_val);
         ctx->check_launch("ws_seed_entries");
-    }
-    PMA_CUDA(cudaMemcpyAsync(bfill, h_fill.data(), nb * 4ull, cudaMemcpyHostToDevice, s));
-    ctx->sync();
-    if (npores) {
         uint32_t* d_seed = buf<uint32_t>(ctx, "ws.seedvox", npores);
         PMA_CUDA(cudaMemcpyAsync(d_seed, seed_voxel.data(), npores * 4, cudaMemcpyHostToDevice, s));
         ws_seed<<<grid_for(ctx, npores), 256, 0, s>>>(d_seed, npores, ws.claim);
         ctx->check_launch("ws_seed");
+        ctx->sync();
     }
+    PMA_CUDA(cudaMemcpyAsync(ws.bfill, h_fill.data(), nb * 4ull, cudaMemcpyHostToDevice, s));
+    ctx->sync();
 
     // Depth sweep (WatershedComputer.cpp:80-102).
-    uint32_t* gv = buf<uint32_t>(ctx, "ws.gv", max_bucket);
-    uint32_t* gpv = buf<uint32_t>(ctx, "ws.gp", max_bucket);
-    uint32_t* nv = buf<uint32_t>(ctx, "ws.nv", max_bucket);
-    uint32_t* npv = buf<uint32_t>(ctx, "ws.np", max_bucket);
+    uint32_t* gvb[2] = {buf<uint32_t>(ctx, "ws.gv0", max_bucket), buf<uint32_t>(ctx, "ws.gv1", max_bucket)};
+    uint32_t* gpb[2] = {buf<uint32_t>(ctx, "ws.gp0", max_bucket), buf<uint32_t>(ctx, "ws.gp1", max_bucket)};
+    const unsigned tgrid = static_cast<unsigned>(ctx->num_sms * 8);
     unsigned long long gen = 0;
-    std::vector<unsigned int> cur_fill(1);
+    unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
     for (int64_t depth = static_cast<int64_t>(nb) - 1; depth >= 0; --depth) {
-        const unsigned long long cap = boff[depth + 1] - boff[depth];
-        if (cap == 0) continue;
-        PMA_CUDA(cudaMemcpyAsync(cur_fill.data(), bfill + depth, 4, cudaMemcpyDeviceToHost, s));
+        if (boff[depth + 1] == boff[depth]) continue;
+        PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + depth, 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
-        size_t ng = cur_fill[0];
-        if (ng == 0) continue;
-        // generation 0: the bucket's entries in time order
-        sort_pairs(ctx, ent_time + boff[depth], srt_time, ent_val + boff[depth], srt_val,
-                   static_cast<int64_t>(ng));
-        ws_unpack_entries<<<grid_for(ctx, ng), 256, 0, s>>>(srt_val, ng, gv, gpv);
+        const size_t n0 = h_small[0];
+        if (n0 == 0) continue;
+        sort_pairs(ctx, ws.ent_time + boff[depth], srt_time, ws.ent_val + boff[depth], srt_val,
+                   static_cast<int64_t>(n0));
+        int cur = 0;
+        ws_unpack_entries<<<grid_for(ctx, n0), 256, 0, s>>>(srt_val, n0, gvb[cur], gpb[cur]);
         ctx->check_launch("ws_unpack_entries");
-        while (ng > 0) {
-            ++gen;
-            const size_t nev = ng * 27;
-            uint32_t* slot_voxel = buf<uint32_t>(ctx, "ws.slots", nev);
-            uint32_t* claimed = buf<uint32_t>(ctx, "ws.claimed", nev);
-            PMA_CUDA(cudaMemsetAsync(slot_voxel, 0xFF, nev * 4, s));
-            const unsigned tg = grid_for(ctx, ng, 128);
-            KernelTimer kt(ctx, "ws_touch");
-            ws_touch<0><<<tg, 128, 0, s>>>(ws, gv, gpv, ng, static_cast<uint32_t>(depth), gen, slot_voxel);
-            ws_touch<1><<<tg, 128, 0, s>>>(ws, gv, gpv, ng, static_cast<uint32_t>(depth), gen, slot_voxel);
-            ws_touch<2><<<tg, 128, 0, s>>>(ws, gv, gpv, ng, static_cast<uint32_t>(depth), gen, slot_voxel);
-            ctx->count_launch(2);
-            ctx->check_launch("ws_touch");
-            const int64_t nc = select_seqs(ctx, SlotTaken{slot_voxel}, nullptr, claimed,
-                                           static_cast<int64_t>(nev), d_count);
-            if (nc == 0) break;
-            ws_distribute<<<grid_for(ctx, nc), 256, 0, s>>>(claimed, nc, slot_voxel, gpv, crad2,
-                                                            static_cast<uint32_t>(depth), gen, d_boff,
-                                                            bfill, ent_time, ent_val);
-            ctx->check_launch("ws_distribute");
-            uint32_t* same = buf<uint32_t>(ctx, "ws.same", nc);
-            const int64_t ns = select_seqs(ctx, AtDepth{slot_voxel, crad2, static_cast<uint32_t>(depth)},
-                                           claimed, same, nc, d_count);
-            if (ns) {
-                ws_next_generation<<<grid_for(ctx, ns), 256, 0, s>>>(same, ns, slot_voxel, gpv, nv, npv);
-                ctx->check_launch("ws_next_generation");
+        h_small[2] = static_cast<unsigned int>(n0);
+        PMA_CUDA(cudaMemcpyAsync(d_ng + cur, &h_small[2], 4, cudaMemcpyHostToDevice, s));
+        KernelTimer kt(ctx, "ws_generations");
+        while (true) {
+            for (int k = 0; k < kGensPerSync; ++k) {
+                ++gen;
+                const int nxt = cur ^ 1;
+                const uint32_t dep = static_cast<uint32_t>(depth);
+                const uint32_t g32 = static_cast<uint32_t>(gen);
+                ws_touch<0><<<tgrid, 128, 0, s>>>(ws, gvb[cur], gpb[cur], d_ng + cur, dep, gen);
+                ws_touch<1><<<tgrid, 128, 0, s>>>(ws, gvb[cur], gpb[cur], d_ng + cur, dep, gen);
+                ws_touch<2><<<tgrid, 128, 0, s>>>(ws, gvb[cur], gpb[cur], d_ng + cur, dep, gen);
+                ws_slot_count<<<tgrid, 256, 0, s>>>(ws.slot_gen, d_ng + cur, g32, ccount);
+                ws_slot_scan<<<1, 1024, 0, s>>>(ccount, d_ng + cur, d_ng + nxt);
+                ws_slot_scatter<<<tgrid, kChunk / 4, 0, s>>>(ws.slot_gen, ws.slot_voxel, d_ng + cur, g32,
+                                                              ccount, gpb[cur], gvb[nxt], gpb[nxt]);
+                ctx->count_launch(6);
+                cur = nxt;
             }
-            std::swap(gv, nv);
-            std::swap(gpv, npv);
-            ng = static_cast<size_t>(ns);
+            PMA_CUDA(cudaGetLastError());
+            PMA_CUDA(cudaMemcpyAsync(h_small + 1, d_ng + cur, 4, cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            if (h_small[1] == 0) break;
+            PMA_REQUIRE(gen < (1ull << 23), PMA_ERR_LIMIT, "pma_watershed: generation limit reached");
         }
     }
     unsigned int h_err = 0;
@@ -415,107 +567,115 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     PMA_REQUIRE(!(h_err & 1u), PMA_ERR_MEMORY, "pma_watershed: shared-voxel records exhausted");
     PMA_REQUIRE(!(h_err & 2u), PMA_ERR_LIMIT, "pma_watershed: more than 7 pores touch one voxel");
 
-    // Volumes and shared voxels.
+    // Volumes, labels and shared voxels.
     auto* pvol = buf<unsigned long long>(ctx, "ws.pvol", npores);
     uint8_t* shared_flag = buf<uint8_t>(ctx, "ws.shared_flag", n);
     PMA_CUDA(cudaMemsetAsync(pvol, 0, std::max<size_t>(npores, 1) * 8, s));
     ws_volumes<<<G, 256, 0, s>>>(ws.claim, ws.ext, n, pvol, shared_flag);
     ctx->check_launch("ws_volumes");
-    uint32_t* sv = buf<uint32_t>(ctx, "ws.sv", n);
-    const int64_t nsh = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), shared_flag, sv,
-                                       static_cast<int64_t>(n), d_count);
-    std::vector<uint32_t> h_claim(nsh), h_pore(nsh * kSlots);
-    std::vector<unsigned long long> h_time(nsh * kSlots);
-    if (nsh) {
-        uint32_t* oc = buf<uint32_t>(ctx, "ws.oc", nsh);
-        uint32_t* op = buf<uint32_t>(ctx, "ws.op", nsh * kSlots);
-        auto* ot = buf<unsigned long long>(ctx, "ws.ot", nsh * kSlots);
-        ws_gather_shared<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.claim, ws.ext, ws.ext_pore,
-                                                            ws.ext_time, oc, op, ot);
-        ctx->check_launch("ws_gather_shared");
-        PMA_CUDA(cudaMemcpyAsync(h_claim.data(), oc, nsh * 4, cudaMemcpyDeviceToHost, s));
-        PMA_CUDA(cudaMemcpyAsync(h_pore.data(), op, nsh * kSlots * 4, cudaMemcpyDeviceToHost, s));
-        PMA_CUDA(cudaMemcpyAsync(h_time.data(), ot, nsh * kSlots * 8, cudaMemcpyDeviceToHost, s));
-    }
-    std::vector<unsigned long long> h_pvol(npores);
-    std::vector<unsigned int> h_pbound(npores);
-    if (npores) {
-        PMA_CUDA(cudaMemcpyAsync(h_pvol.data(), pvol, npores * 8, cudaMemcpyDeviceToHost, s));
-        PMA_CUDA(cudaMemcpyAsync(h_pbound.data(), ws.pbound, npores * 4, cudaMemcpyDeviceToHost, s));
-    }
-    ctx->sync();
-
-    // Keys of shared voxels and their creation times (host; shared voxels are few).
-    struct KeyInfo {
-        unsigned long long created = kNoTime;
-        unsigned long long volume = 0;
-    };
-    std::map<std::vector<uint32_t>, KeyInfo> keys;
-    std::vector<const std::vector<uint32_t>*> final_key(nsh);
-    std::vector<std::pair<unsigned long long, uint32_t>> ext;
-    for (int64_t i = 0; i < nsh; ++i) {
-        ext.clear();
-        for (int k = 0; k < kSlots; ++k) {
-            const uint32_t p = h_pore[i * kSlots + k];
-            if (p != kNone) ext.push_back({h_time[i * kSlots + k], p});
-        }
-        std::sort(ext.begin(), ext.end());
-        std::vector<uint32_t> key;
-        key.push_back(pores[ext[0].second].id);
-        key.push_back(pores[h_claim[i] - 1].id);
-        auto it = keys.emplace(key, KeyInfo()).first;
-        it->second.created = std::min(it->second.created, ext[0].first);
-        for (size_t k = 1; k < ext.size(); ++k) {
-            key.push_back(pores[ext[k].second].id);
-            it = keys.emplace(key, KeyInfo()).first;
-            it->second.created = std::min(it->second.created, ext[k].first);
-        }
-        it->second.volume++;
-        final_key[i] = &it->first;
-    }
-    std::vector<std::pair<unsigned long long, const std::vector<uint32_t>*>> by_time;
-    for (auto& kv : keys) by_time.push_back({kv.second.created, &kv.first});
-    std::sort(by_time.begin(), by_time.end());
-    std::map<const std::vector<uint32_t>*, uint32_t> key_id;
-    for (size_t k = 0; k < by_time.size(); ++k)
-        key_id[by_time[k].second] = 0xFFFFFFFFu - 1u - static_cast<uint32_t>(k);
-
-    // Labels.
     std::vector<uint32_t> pore_id(std::max<size_t>(npores, 1));
     for (size_t k = 0; k < npores; ++k) pore_id[k] = pores[k].id;
     uint32_t* d_pid = buf<uint32_t>(ctx, "ws.pid", pore_id.size());
     PMA_CUDA(cudaMemcpyAsync(d_pid, pore_id.data(), pore_id.size() * 4, cudaMemcpyHostToDevice, s));
     ws_labels<<<G, 256, 0, s>>>(ws.claim, n, d_pid, labels);
     ctx->check_launch("ws_labels");
-    if (nsh) {
-        std::vector<uint32_t> sid(nsh);
-        for (int64_t i = 0; i < nsh; ++i) sid[i] = key_id[final_key[i]];
-        uint32_t* d_sid = buf<uint32_t>(ctx, "ws.sid", nsh);
-        PMA_CUDA(cudaMemcpyAsync(d_sid, sid.data(), nsh * 4, cudaMemcpyHostToDevice, s));
-        ws_shared_labels<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, d_sid, nsh, labels);
-        ctx->check_launch("ws_shared_labels");
-    }
-    ctx->sync();
+    uint32_t* sv = buf<uint32_t>(ctx, "ws.sv", n);
+    const int64_t nsh = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), shared_flag, sv,
+                                       static_cast<int64_t>(n), d_count);
 
     pma_table* t = new pma_table;
+    std::vector<unsigned long long> h_pvol(npores);
+    std::vector<unsigned int> h_pbound(npores);
+    if (npores) {
+        PMA_CUDA(cudaMemcpyAsync(h_pvol.data(), pvol, npores * 8, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaMemcpyAsync(h_pbound.data(), ws.pbound, npores * 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+    }
     for (size_t k = 0; k < npores; ++k) {
         pma_pore p = pores[k];
         p.volume = h_pvol[k];
         p.is_boundary = h_pbound[k] ? 1 : 0;
         t->pores.push_back(p);
     }
-    std::vector<std::pair<uint32_t, const std::vector<uint32_t>*>> rows;
-    for (auto& kv : key_id) rows.push_back({kv.second, kv.first});
-    std::sort(rows.begin(), rows.end(),
-              [](const std::pair<uint32_t, const std::vector<uint32_t>*>& a,
-                 const std::pair<uint32_t, const std::vector<uint32_t>*>& b) { return a.first < b.first; });
-    for (auto& r : rows) {
+    if (nsh == 0) return t;
+
+    // Shared types on the device.
+    const size_t nrec = static_cast<size_t>(nsh) * kSlots;
+    PMA_REQUIRE(nrec < 0xFFFFFFFFull, PMA_ERR_LIMIT, "pma_watershed: too many shared voxels");
+    uint32_t* kseq = buf<uint32_t>(ctx, "ws.kseq", static_cast<size_t>(nsh) * kKey);
+    uint8_t* klen = buf<uint8_t>(ctx, "ws.klen", nsh);
+    auto* rh1 = buf<unsigned long long>(ctx, "ws.rh1", nrec);
+    auto* rh2 = buf<unsigned long long>(ctx, "ws.rh2", nrec);
+    auto* rtime = buf<unsigned long long>(ctx, "ws.rtime", nrec);
+    uint8_t* rvalid = buf<uint8_t>(ctx, "ws.rvalid", nrec);
+    ws_keys<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.claim, ws.ext, ws.ext_pore, ws.ext_time, kseq,
+                                               klen, rh1, rh2, rtime, rvalid);
+    ctx->check_launch("ws_keys");
+    uint32_t* rec = buf<uint32_t>(ctx, "ws.rec", nrec);
+    const int64_t nr = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), rvalid, rec,
+                                      static_cast<int64_t>(nrec), d_count);
+    // equal prefixes become adjacent: stable sorts by h2, then by h1 (values: record ids)
+    auto* kh = buf<unsigned long long>(ctx, "ws.kh", nr);
+    auto* kh2 = buf<unsigned long long>(ctx, "ws.kh2", nr);
+    uint32_t* rec2 = buf<uint32_t>(ctx, "ws.rec2", nr);
+    ws_gather_h<<<grid_for(ctx, nr), 256, 0, s>>>(rh2, rec, nr, kh);
+    ctx->check_launch("ws_gather_h");
+    sort_pairs(ctx, kh, kh2, rec, rec2, nr);
+    ws_gather_h<<<grid_for(ctx, nr), 256, 0, s>>>(rh1, rec2, nr, kh);
+    ctx->check_launch("ws_gather_h");
+    sort_pairs(ctx, kh, kh2, rec2, rec, nr);
+    uint32_t* gstart = buf<uint32_t>(ctx, "ws.gstart", nr);
+    uint32_t* gexcl = buf<uint32_t>(ctx, "ws.gexcl", nr);
+    ws_group_starts<<<grid_for(ctx, nr), 256, 0, s>>>(rec, nr, rh1, rh2, kseq, gstart, ws.err);
+    ctx->check_launch("ws_group_starts");
+    exclusive_sum(ctx, gstart, gexcl, nr);
+    uint32_t last[2] = {0, 0};
+    PMA_CUDA(cudaMemcpyAsync(&last[0], gexcl + nr - 1, 4, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(&last[1], gstart + nr - 1, 4, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(&h_err, ws.err, 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    PMA_REQUIRE(!(h_err & 4u), PMA_ERR_INTERNAL, "pma_watershed: shared-type hash collision");
+    const int64_t ngr = static_cast<int64_t>(last[0]) + last[1];
+    auto* gtime = buf<unsigned long long>(ctx, "ws.gtime", ngr);
+    auto* gvol = buf<unsigned long long>(ctx, "ws.gvol", ngr);
+    uint32_t* grep = buf<uint32_t>(ctx, "ws.grep", ngr);
+    uint32_t* final_group = buf<uint32_t>(ctx, "ws.fgroup", nsh);
+    PMA_CUDA(cudaMemsetAsync(gtime, 0xFF, ngr * 8, s));
+    PMA_CUDA(cudaMemsetAsync(gvol, 0, ngr * 8, s));
+    ws_group_reduce<<<grid_for(ctx, nr), 256, 0, s>>>(rec, gexcl, gstart, nr, rtime, klen, gtime, gvol, grep,
+                                                      final_group);
+    ctx->check_launch("ws_group_reduce");
+    uint32_t* rows = buf<uint32_t>(ctx, "ws.rows", static_cast<size_t>(ngr) * kKey);
+    ws_group_rows<<<grid_for(ctx, ngr), 256, 0, s>>>(grep, ngr, kseq, rows);
+    ctx->check_launch("ws_group_rows");
+    std::vector<unsigned long long> h_gtime(ngr), h_gvol(ngr);
+    std::vector<uint32_t> h_rows(static_cast<size_t>(ngr) * kKey);
+    PMA_CUDA(cudaMemcpyAsync(h_gtime.data(), gtime, ngr * 8, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(h_gvol.data(), gvol, ngr * 8, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(h_rows.data(), rows, h_rows.size() * 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    // ids in creation order
+    std::vector<uint32_t> order(ngr);
+    for (int64_t i = 0; i < ngr; ++i) order[i] = static_cast<uint32_t>(i);
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return h_gtime[a] < h_gtime[b]; });
+    std::vector<uint32_t> gid(ngr);
+    for (int64_t k = 0; k < ngr; ++k) gid[order[k]] = 0xFFFFFFFFu - 1u - static_cast<uint32_t>(k);
+    uint32_t* d_gid = buf<uint32_t>(ctx, "ws.gid", ngr);
+    PMA_CUDA(cudaMemcpyAsync(d_gid, gid.data(), ngr * 4, cudaMemcpyHostToDevice, s));
+    ws_shared_labels<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, final_group, d_gid, nsh, labels);
+    ctx->check_launch("ws_shared_labels");
+    ctx->sync();
+    // rows in id order (ascending id = reverse creation order)
+    for (int64_t k = ngr - 1; k >= 0; --k) {
+        const uint32_t gi = order[k];
         pma_throat th;
-        th.id = r.first;
-        th.n_pores = static_cast<uint32_t>(r.second->size());
-        th.volume = keys[*r.second].volume;
+        th.id = gid[gi];
+        th.volume = h_gvol[gi];
         th.pool_offset = t->pool.size();
-        t->pool.insert(t->pool.end(), r.second->begin(), r.second->end());
+        uint32_t L = 0;
+        for (int j = 0; j < kKey && h_rows[static_cast<size_t>(gi) * kKey + j] != kNone; ++j, ++L)
+            t->pool.push_back(pore_id[h_rows[static_cast<size_t>(gi) * kKey + j]]);
+        th.n_pores = L;
         t->throats.push_back(th);
     }
     return t;
