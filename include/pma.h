@@ -86,6 +86,23 @@ typedef struct pma_edt_stats {
 int pma_edt(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, uint32_t* d_edt2,
             pma_edt_stats* stats, uint64_t* h_hist, size_t hist_cap);
 
+/* Allocation-free variant of pma_edt. No counterpart in the reference: it gives the same
+ * results as pma_edt (EuclideanDistanceComputer.cpp:30-44) for callers that cannot let
+ * the library allocate device memory. It takes no context, calls no allocator and runs
+ * on the calling thread's current device, on cuda_stream (NULL = the legacy default
+ * stream); it returns once that stream's work for the call is complete.
+ * Its only scratch, the histogram bins and the maximum, is a fixed array of
+ * PMA_EDT_NOALLOC_MAX_HIST_BINS 64-bit counters (2 MiB) in the library's global memory,
+ * cleared by every call. Volumes whose smallest extent is above 1024 need more bins and
+ * are rejected with PMA_ERR_LIMIT.
+ * The first call on a device looks up the scratch address on that device (set-up); make
+ * that first call before any stream capture. All calls on one device share the scratch:
+ * calls that overlap in time (from several host threads, or on streams not ordered with
+ * each other) race on it and return wrong statistics. */
+#define PMA_EDT_NOALLOC_MAX_HIST_BINS 262144
+int pma_edt_noalloc(const uint8_t* d_solid, pma_dims dims, uint32_t* d_edt2,
+                    pma_edt_stats* stats, uint64_t* h_hist, size_t hist_cap, void* cuda_stream);
+
 /* Containing-ball radii (squared), the winning centre of each void voxel and the
  * IsMaximumBall mask (0 solid, 127 inner, 255 outer). Replaces
  * ContainingBallsAssigner::SetContainingBalls (ContainingBallsAssigner.cpp:36-60;

@@ -77,6 +77,8 @@ _SIGNATURES = {
     "pma_ctx_trim": (ctypes.c_int, [ctypes.c_void_p]),
     "pma_edt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_void_p,
                                ctypes.POINTER(EdtStats), ctypes.c_void_p, ctypes.c_size_t]),
+    "pma_edt_noalloc": (ctypes.c_int, [ctypes.c_void_p, Dims, ctypes.c_void_p, ctypes.POINTER(EdtStats),
+                                       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "pma_containing_balls": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_uint32,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_void_p, c_u64p]),

@@ -194,6 +194,14 @@ int pma_edt(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, uint32_t* d_edt
     });
 }
 
+int pma_edt_noalloc(const uint8_t* d_solid, pma_dims dims, uint32_t* d_edt2, pma_edt_stats* stats,
+                    uint64_t* h_hist, size_t hist_cap, void* cuda_stream) {
+    return guarded([&] {
+        pma::edt_noalloc(d_solid, dims, d_edt2, stats, h_hist, hist_cap,
+                         static_cast<cudaStream_t>(cuda_stream));
+    });
+}
+
 int pma_containing_balls(pma_ctx* ctx, const uint32_t* d_edt2, pma_dims dims, uint32_t max_edt2,
                          uint32_t* d_crad2, uint32_t* d_cx, uint32_t* d_cy, uint32_t* d_cz,
                          uint8_t* d_mask, uint64_t* h_count) {

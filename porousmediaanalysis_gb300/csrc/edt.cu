@@ -12,6 +12,9 @@
 //   pass Z: tiles of 16 consecutive y by all z staged in shared memory, same exact scan,
 //           fused with the running maximum and the histogram of balls that do not cross
 //           the image boundary (EDC.cpp:310-327).
+#include <algorithm>
+#include <mutex>
+
 #include "pma_internal.h"
 
 namespace pma {
@@ -247,6 +250,130 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
         size_t want = std::min<size_t>(hist_cap, static_cast<size_t>(maxv) + 1);
         size_t have = std::min(want, hist_len);
         PMA_CUDA(cudaMemcpy(h_hist, d_hist, have * 8, cudaMemcpyDeviceToHost));
+        for (size_t i = have; i < want; ++i) h_hist[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant (pma_edt_noalloc)
+//
+// Some callers cannot let the library allocate device memory: an application whose own
+// memory pool already holds the device's memory, or one that must not call cudaMalloc and
+// cudaFree while it runs because both can synchronise the whole device and stall its other
+// streams (a service answering requests on streams it owns, an interactive viewer stepping
+// through volumes). Such callers also hold no pma_ctx, whose scratch cache allocates on
+// first use. This variant writes its results into the caller's buffers and keeps its only
+// scratch - the histogram bins and the running maximum of pass Z - in a fixed array in the
+// module's global memory. Its size bounds the volumes it accepts: a 2^18-bin histogram
+// covers balls up to e = 511^2, i.e. volumes whose smallest extent is at most 1024.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocHistBins = size_t(1) << 18;
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocDevice {
+    unsigned long long* scratch = nullptr;  // address of the static array on that device
+    size_t smem_optin = 0;
+    int num_sms = 0;
+};
+
+std::mutex g_noalloc_mutex;
+NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+
+}  // namespace
+
+// Bins [0, kNoAllocHistBins) followed by two words; the maximum sits in the first word
+// after the bins in use (hist_len), as in the context-based path.
+static __device__ __align__(256) unsigned long long g_edt_noalloc_scratch[kNoAllocHistBins + 2];
+
+// Once per device, with that device current: the scratch address, the shared-memory limit
+// and the SM count. Later calls read the cached values.
+static NoAllocDevice noalloc_device() {
+    int dev = 0;
+    PMA_CUDA(cudaGetDevice(&dev));
+    PMA_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, PMA_ERR_ARGUMENT,
+                "pma_edt_noalloc: device ordinal above 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoAllocDevice& e = g_noalloc_devices[dev];
+    if (!e.scratch) {
+        void* p = nullptr;
+        const cudaError_t rc = cudaGetSymbolAddress(&p, g_edt_noalloc_scratch);
+        PMA_REQUIRE(rc == cudaSuccess && p, PMA_ERR_CUDA,
+                    std::string("pma_edt_noalloc: cudaGetSymbolAddress of the scratch array failed: ") +
+                        cudaGetErrorString(rc));
+        int optin = 0;
+        PMA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        PMA_CUDA(cudaDeviceGetAttribute(&e.num_sms, cudaDevAttrMultiProcessorCount, dev));
+        e.smem_optin = static_cast<size_t>(optin);
+        e.scratch = static_cast<unsigned long long*>(p);
+    }
+    return e;
+}
+
+void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats* stats,
+                 uint64_t* h_hist, size_t hist_cap, cudaStream_t s) {
+    check_dims(d);
+    PMA_REQUIRE(solid && edt2, PMA_ERR_ARGUMENT, "pma_edt_noalloc: null device pointer");
+    const int SX = d.sx, SY = d.sy, SZ = d.sz;
+    const int minext = std::min(SX, std::min(SY, SZ));
+    size_t hist_len = static_cast<size_t>((minext - 1) / 2) * ((minext - 1) / 2) + 1;
+    hist_len = std::max<size_t>(hist_len, kHistSmall);
+    PMA_REQUIRE(hist_len <= kNoAllocHistBins, PMA_ERR_LIMIT,
+                "pma_edt_noalloc: smallest volume extent " + std::to_string(minext) +
+                    " is above 1024, the largest its fixed 2 MiB histogram scratch covers; use pma_edt");
+    const NoAllocDevice dev = noalloc_device();
+
+    {
+        const int words = (SX + 31) / 32;
+        int threads = 256;
+        while (threads > 32 && static_cast<size_t>(words) * 4 * threads > 96 * 1024) threads >>= 1;
+        const size_t smem = static_cast<size_t>(words) * 4 * threads;
+        PMA_REQUIRE(smem <= dev.smem_optin, PMA_ERR_ARGUMENT, "pma_edt_noalloc: X extent too large");
+        PMA_CUDA(cudaFuncSetAttribute(edt_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+        const size_t cols = static_cast<size_t>(SY) * SZ;
+        edt_pass_x<<<div_up(cols, threads), threads, smem, s>>>(solid, edt2, SX, SY, SZ, words);
+        PMA_CUDA(cudaGetLastError());
+    }
+    {
+        int warps = 8;
+        while (warps > 1 && static_cast<size_t>(warps) * SY * 4 > 96 * 1024) warps >>= 1;
+        const size_t smem = static_cast<size_t>(warps) * SY * 4;
+        PMA_REQUIRE(smem <= dev.smem_optin, PMA_ERR_ARGUMENT, "pma_edt_noalloc: Y extent too large");
+        PMA_CUDA(cudaFuncSetAttribute(edt_pass_y, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+        const size_t rows = static_cast<size_t>(SX) * SZ;
+        const size_t blocks = std::min<size_t>((rows + warps - 1) / warps, static_cast<size_t>(dev.num_sms) * 64);
+        edt_pass_y<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(edt2, SY, rows);
+        PMA_CUDA(cudaGetLastError());
+    }
+    // The bins in use and the maximum word must start at zero on every call.
+    unsigned long long* d_hist = dev.scratch;
+    auto* d_max = reinterpret_cast<unsigned int*>(d_hist + hist_len);
+    PMA_CUDA(cudaMemsetAsync(d_hist, 0, hist_len * 8 + 16, s));
+    {
+        const size_t smem = static_cast<size_t>(SZ) * kTileY * 4 + kHistSmall * 4;
+        PMA_REQUIRE(smem <= dev.smem_optin, PMA_ERR_ARGUMENT, "pma_edt_noalloc: Z extent too large");
+        PMA_CUDA(cudaFuncSetAttribute(edt_pass_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+        const size_t tiles = static_cast<size_t>(SX) * ((SY + kTileY - 1) / kTileY);
+        edt_pass_z<<<static_cast<unsigned>(tiles), 256, smem, s>>>(edt2, SX, SY, SZ, d_hist, hist_len, d_max);
+        PMA_CUDA(cudaGetLastError());
+    }
+    unsigned int maxv = 0;
+    PMA_CUDA(cudaMemcpyAsync(&maxv, d_max, 4, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaStreamSynchronize(s));
+    if (stats) {
+        stats->max_edt2 = maxv;
+        stats->pad_ = 0;
+        stats->hist_len = static_cast<uint64_t>(maxv) + 1;
+    }
+    if (h_hist && hist_cap) {
+        const size_t want = std::min<size_t>(hist_cap, static_cast<size_t>(maxv) + 1);
+        const size_t have = std::min(want, hist_len);
+        PMA_CUDA(cudaMemcpyAsync(h_hist, d_hist, have * 8, cudaMemcpyDeviceToHost, s));
+        PMA_CUDA(cudaStreamSynchronize(s));
         for (size_t i = have; i < want; ++i) h_hist[i] = 0;
     }
 }

@@ -124,6 +124,8 @@ inline size_t voxels(pma_dims d) { return static_cast<size_t>(d.sx) * d.sy * d.s
 // Stage implementations (device pointers, ctx stream).
 void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats* stats,
          uint64_t* h_hist, size_t hist_cap);
+void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats* stats,
+                 uint64_t* h_hist, size_t hist_cap, cudaStream_t s);
 void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t max_edt2,
                       uint32_t* crad2, uint32_t* cx, uint32_t* cy, uint32_t* cz, uint8_t* mask,
                       uint64_t* count);
