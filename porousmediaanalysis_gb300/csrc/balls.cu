@@ -16,10 +16,12 @@
 // (sqrt(R) + sqrt(k))^2 <= R'.
 //
 // Gather: the volume is cut into 8^3 tiles; every kept centre is listed in each tile its
-// ball reaches. One CTA per tile sorts its list by key in shared memory (descending), and
-// each voxel takes the first entry whose ball covers it: that entry is the covering centre
-// of largest key, i.e. the reference's winner. A voxel stops at its winner, so the work is
-// the winner's rank in the tile list rather than the ball volumes a scatter would touch.
+// ball reaches, unless its key is below the tile's floor (the largest key of a ball covering
+// the whole tile, which every voxel of the tile is covered by). One CTA per tile sorts its
+// list by key in shared memory (descending), and each voxel takes the first entry whose ball
+// covers it: that entry is the covering centre of largest key, i.e. the reference's winner.
+// A voxel stops at its winner, so the work is the winner's rank in the tile list rather than
+// the ball volumes a scatter would touch.
 #include <thrust/iterator/counting_iterator.h>
 
 #include <vector>
@@ -124,7 +126,9 @@ struct Tiles {
 };
 
 // Visits the tiles whose box is within sqrt(R) of centre (x, y, z), restricted to tile
-// z-range [tz0, tz1).
+// z-range [tz0, tz1). f(tile, full): full = the ball covers the whole tile (clipped to the
+// volume), i.e. its farthest corner - a ball is convex, so covering the eight corners of a
+// box covers every lattice point in it.
 template <class F>
 __device__ __forceinline__ void for_each_tile(Grid g, Tiles t, int x, int y, int z, uint32_t R,
                                               int tz0, int tz1, F f) {
@@ -133,51 +137,92 @@ __device__ __forceinline__ void for_each_tile(Grid g, Tiles t, int x, int y, int
     const int ay = max(y - r, 0) / kTile, by = min(y + r, g.SY - 1) / kTile;
     const int az = max(max(z - r, 0) / kTile, tz0), bz = min(min(z + r, g.SZ - 1) / kTile, tz1 - 1);
     for (int tz = az; tz <= bz; ++tz) {
-        const int lz = tz * kTile, hz = lz + kTile - 1;
+        const int lz = tz * kTile, hz = min(lz + kTile - 1, g.SZ - 1);
         const int dz = z < lz ? lz - z : (z > hz ? z - hz : 0);
+        const int fz = max(abs(z - lz), abs(hz - z));
         for (int tx = ax; tx <= bx; ++tx) {
-            const int lx = tx * kTile, hx = lx + kTile - 1;
+            const int lx = tx * kTile, hx = min(lx + kTile - 1, g.SX - 1);
             const int dx = x < lx ? lx - x : (x > hx ? x - hx : 0);
             const int dxz = dx * dx + dz * dz;
             if (static_cast<uint32_t>(dxz) > R) continue;
+            const int fx = max(abs(x - lx), abs(hx - x));
+            const int fxz = fx * fx + fz * fz;
             for (int ty = ay; ty <= by; ++ty) {
-                const int ly = ty * kTile, hy = ly + kTile - 1;
+                const int ly = ty * kTile, hy = min(ly + kTile - 1, g.SY - 1);
                 const int dy = y < ly ? ly - y : (y > hy ? y - hy : 0);
-                if (static_cast<uint32_t>(dxz + dy * dy) <= R) f(t.id(tx, ty, tz));
+                if (static_cast<uint32_t>(dxz + dy * dy) > R) continue;
+                const int fy = max(abs(y - ly), abs(hy - y));
+                f(t.id(tx, ty, tz), static_cast<uint32_t>(fxz + fy * fy) <= R);
             }
         }
     }
 }
 
+// Floor of a tile: the largest key among balls covering the whole tile. Every voxel of the
+// tile is covered by that ball, so its winner's key is at least the floor, and list entries
+// below it can be left out.
+struct FloorTile {
+    unsigned long long* floor;
+    unsigned long long key;
+    __device__ void operator()(size_t tid, bool full) const {
+        if (full) atomicMax(&floor[tid], key);
+    }
+};
+
 struct CountTile {
+    const unsigned long long* floor;
     unsigned int* tcount;
-    __device__ void operator()(size_t tid) const { atomicAdd(&tcount[tid], 1u); }
+    unsigned long long key;
+    __device__ void operator()(size_t tid, bool) const {
+        if (key >= __ldg(floor + tid)) atomicAdd(&tcount[tid], 1u);
+    }
 };
 
 struct FillTile {
+    const unsigned long long* floor;
     const unsigned long long* toff;
     unsigned long long base;
     unsigned int* tcursor;
     unsigned long long* entries;
     unsigned long long key;
-    __device__ void operator()(size_t tid) const {
+    __device__ void operator()(size_t tid, bool) const {
+        if (key < __ldg(floor + tid)) return;
         const unsigned pos = atomicAdd(&tcursor[tid], 1u);
         entries[toff[tid] - base + pos] = key;
     }
 };
 
-__global__ void balls_tile_count(const uint32_t* __restrict__ edt2, const uint32_t* __restrict__ cand,
-                                 size_t nc, Grid g, Tiles t, unsigned int* __restrict__ tcount) {
+__device__ __forceinline__ unsigned long long ball_key(Grid g, int x, int y, int z, uint32_t R) {
+    const uint32_t lex = (static_cast<uint32_t>(x) * g.SY + y) * static_cast<uint32_t>(g.SZ) + z;
+    return (static_cast<unsigned long long>(R) << 32) | (0xFFFFFFFFu - lex);
+}
+
+__global__ void balls_tile_floor(const uint32_t* __restrict__ edt2, const uint32_t* __restrict__ cand,
+                                 size_t nc, Grid g, Tiles t, unsigned long long* __restrict__ floor) {
     PMA_GRID_STRIDE(i, nc) {
         const uint32_t v = cand[i];
         int x, y, z;
         g.coords(v, x, y, z);
-        for_each_tile(g, t, x, y, z, edt2[v], 0, t.TZ, CountTile{tcount});
+        const uint32_t R = edt2[v];
+        for_each_tile(g, t, x, y, z, R, 0, t.TZ, FloorTile{floor, ball_key(g, x, y, z, R)});
+    }
+}
+
+__global__ void balls_tile_count(const uint32_t* __restrict__ edt2, const uint32_t* __restrict__ cand,
+                                 size_t nc, Grid g, Tiles t, const unsigned long long* __restrict__ floor,
+                                 unsigned int* __restrict__ tcount) {
+    PMA_GRID_STRIDE(i, nc) {
+        const uint32_t v = cand[i];
+        int x, y, z;
+        g.coords(v, x, y, z);
+        const uint32_t R = edt2[v];
+        for_each_tile(g, t, x, y, z, R, 0, t.TZ, CountTile{floor, tcount, ball_key(g, x, y, z, R)});
     }
 }
 
 __global__ void balls_tile_fill(const uint32_t* __restrict__ edt2, const uint32_t* __restrict__ cand,
                                 size_t nc, Grid g, Tiles t, int tz0, int tz1,
+                                const unsigned long long* __restrict__ floor,
                                 const unsigned long long* __restrict__ toff, unsigned long long base,
                                 unsigned int* __restrict__ tcursor, unsigned long long* __restrict__ entries) {
     PMA_GRID_STRIDE(i, nc) {
@@ -185,9 +230,8 @@ __global__ void balls_tile_fill(const uint32_t* __restrict__ edt2, const uint32_
         int x, y, z;
         g.coords(v, x, y, z);
         const uint32_t R = edt2[v];
-        const uint32_t lex = (static_cast<uint32_t>(x) * g.SY + y) * static_cast<uint32_t>(g.SZ) + z;
-        const unsigned long long key = (static_cast<unsigned long long>(R) << 32) | (0xFFFFFFFFu - lex);
-        for_each_tile(g, t, x, y, z, R, tz0, tz1, FillTile{toff, base, tcursor, entries, key});
+        for_each_tile(g, t, x, y, z, R, tz0, tz1,
+                      FillTile{floor, toff, base, tcursor, entries, ball_key(g, x, y, z, R)});
     }
 }
 
@@ -382,11 +426,15 @@ void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t m
     unsigned int* tcount = buf<unsigned int>(ctx, "balls.tcount", ntiles);
     unsigned int* tcursor = buf<unsigned int>(ctx, "balls.tcursor", ntiles);
     auto* toff = buf<unsigned long long>(ctx, "balls.toff", ntiles + 1);
+    auto* floor = buf<unsigned long long>(ctx, "balls.floor", ntiles);
     PMA_CUDA(cudaMemsetAsync(tcount, 0, ntiles * 4, s));
     PMA_CUDA(cudaMemsetAsync(tcursor, 0, ntiles * 4, s));
+    PMA_CUDA(cudaMemsetAsync(floor, 0, ntiles * 8, s));
     if (nc) {
         KernelTimer kt(ctx, "balls_tile_count");
-        balls_tile_count<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, tcount);
+        balls_tile_floor<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, floor);
+        ctx->check_launch("balls_tile_floor");
+        balls_tile_count<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, floor, tcount);
         ctx->check_launch("balls_tile_count");
     }
     std::vector<unsigned int> hc(ntiles);
@@ -407,8 +455,8 @@ void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t m
         auto* entries = buf<unsigned long long>(ctx, "balls.entries", cnt);
         if (nc) {
             KernelTimer kt(ctx, "balls_tile_fill");
-            balls_tile_fill<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, z0, z1, toff, base,
-                                                              tcursor, entries);
+            balls_tile_fill<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, z0, z1, floor, toff,
+                                                              base, tcursor, entries);
             ctx->check_launch("balls_tile_fill");
         }
         {

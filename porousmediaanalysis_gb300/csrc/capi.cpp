@@ -40,6 +40,14 @@ void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
     return b.ptr;
 }
 
+void pma_ctx::release(const std::string& tag) {
+    auto it = cache.find(tag);
+    if (it == cache.end()) return;
+    PMA_CUDA(cudaStreamSynchronize(stream));
+    if (it->second.ptr) PMA_CUDA(cudaFree(it->second.ptr));
+    cache.erase(it);
+}
+
 void* pma_ctx::host_staging(size_t bytes) {
     if (pinned_bytes >= bytes && pinned) return pinned;
     if (pinned) {
@@ -96,6 +104,8 @@ int pma_ctx_create(int device, pma_ctx** out) {
 int pma_ctx_destroy(pma_ctx* ctx) {
     if (!ctx) return PMA_OK;
     return guarded([&] {
+        for (pma_ctx* lane : ctx->lanes) pma_ctx_destroy(lane);
+        ctx->lanes.clear();
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
         for (auto& kv : ctx->cache)
@@ -124,7 +134,12 @@ int pma_ctx_set_stream(pma_ctx* ctx, void* stream) {
     });
 }
 
-uint64_t pma_ctx_launch_count(const pma_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
+uint64_t pma_ctx_launch_count(const pma_ctx* ctx) {
+    if (!ctx) return 0;
+    uint64_t total = ctx->launches.load();
+    for (const pma_ctx* lane : ctx->lanes) total += pma_ctx_launch_count(lane);
+    return total;
+}
 
 int pma_ctx_set_timing(pma_ctx* ctx, int enable) {
     return guarded([&] {
@@ -169,14 +184,17 @@ size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap) {
 
 size_t pma_ctx_scratch_bytes(const pma_ctx* ctx) {
     size_t s = 0;
-    if (ctx)
+    if (ctx) {
         for (auto& kv : ctx->cache) s += kv.second.bytes;
+        for (const pma_ctx* lane : ctx->lanes) s += pma_ctx_scratch_bytes(lane);
+    }
     return s;
 }
 
 int pma_ctx_trim(pma_ctx* ctx) {
     return guarded([&] {
         PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
+        for (pma_ctx* lane : ctx->lanes) PMA_REQUIRE(pma_ctx_trim(lane) == PMA_OK, PMA_ERR_CUDA, "pma_ctx_trim: lane");
         PMA_CUDA(cudaSetDevice(ctx->device));
         PMA_CUDA(cudaStreamSynchronize(ctx->stream));
         for (auto& kv : ctx->cache)

@@ -14,6 +14,7 @@
 //           the image boundary (EDC.cpp:310-327).
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "pma_internal.h"
 
@@ -183,11 +184,30 @@ __global__ void edt_pass_z(uint32_t* __restrict__ g, int SX, int SY, int SZ,
         if (h_small[i]) atomicAdd(&hist[i], static_cast<unsigned long long>(h_small[i]));
 }
 
+// The dynamic shared-memory limit is a process-wide attribute of each kernel, so it is set
+// once per device to the device's opt-in maximum: lowering it per call would race with
+// calls on other host threads (batch lanes) that launch with more.
+std::mutex g_attr_mutex;
+std::vector<int> g_attr_devices;
+
+void edt_smem_attributes(size_t optin) {
+    int dev = 0;
+    PMA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    if (std::find(g_attr_devices.begin(), g_attr_devices.end(), dev) != g_attr_devices.end()) return;
+    const int bytes = static_cast<int>(optin);
+    PMA_CUDA(cudaFuncSetAttribute(edt_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    PMA_CUDA(cudaFuncSetAttribute(edt_pass_y, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    PMA_CUDA(cudaFuncSetAttribute(edt_pass_z, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    g_attr_devices.push_back(dev);
+}
+
 }  // namespace
 
 void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats* stats,
          uint64_t* h_hist, size_t hist_cap) {
     check_dims(d);
+    edt_smem_attributes(ctx->smem_optin);
     PMA_REQUIRE(solid && edt2, PMA_ERR_ARGUMENT, "pma_edt: null device pointer");
     const int SX = d.sx, SY = d.sy, SZ = d.sz;
     cudaStream_t s = ctx->stream;
@@ -199,8 +219,6 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
         while (threads > 32 && static_cast<size_t>(words) * 4 * threads > 96 * 1024) threads >>= 1;
         const size_t smem = static_cast<size_t>(words) * 4 * threads;
         PMA_REQUIRE(smem <= ctx->smem_optin, PMA_ERR_ARGUMENT, "pma_edt: X extent too large");
-        PMA_CUDA(cudaFuncSetAttribute(edt_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
         const size_t cols = static_cast<size_t>(SY) * SZ;
         KernelTimer kt(ctx, "edt_pass_x");
         edt_pass_x<<<div_up(cols, threads), threads, smem, s>>>(solid, edt2, SX, SY, SZ, words);
@@ -212,8 +230,6 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
         while (warps > 1 && static_cast<size_t>(warps) * SY * 4 > 96 * 1024) warps >>= 1;
         const size_t smem = static_cast<size_t>(warps) * SY * 4;
         PMA_REQUIRE(smem <= ctx->smem_optin, PMA_ERR_ARGUMENT, "pma_edt: Y extent too large");
-        PMA_CUDA(cudaFuncSetAttribute(edt_pass_y, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
         const size_t rows = static_cast<size_t>(SX) * SZ;
         size_t blocks = std::min<size_t>((rows + warps - 1) / warps, static_cast<size_t>(ctx->num_sms) * 64);
         KernelTimer kt(ctx, "edt_pass_y");
@@ -230,8 +246,6 @@ void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt
     {
         const size_t smem = static_cast<size_t>(SZ) * kTileY * 4 + kHistSmall * 4;
         PMA_REQUIRE(smem <= ctx->smem_optin, PMA_ERR_ARGUMENT, "pma_edt: Z extent too large");
-        PMA_CUDA(cudaFuncSetAttribute(edt_pass_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
         const size_t tiles = static_cast<size_t>(SX) * ((SY + kTileY - 1) / kTileY);
         KernelTimer kt(ctx, "edt_pass_z");
         edt_pass_z<<<static_cast<unsigned>(tiles), 256, smem, s>>>(edt2, SX, SY, SZ, d_hist,
@@ -323,6 +337,7 @@ void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats
                 "pma_edt_noalloc: smallest volume extent " + std::to_string(minext) +
                     " is above 1024, the largest its fixed 2 MiB histogram scratch covers; use pma_edt");
     const NoAllocDevice dev = noalloc_device();
+    edt_smem_attributes(dev.smem_optin);
 
     {
         const int words = (SX + 31) / 32;
@@ -330,8 +345,6 @@ void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats
         while (threads > 32 && static_cast<size_t>(words) * 4 * threads > 96 * 1024) threads >>= 1;
         const size_t smem = static_cast<size_t>(words) * 4 * threads;
         PMA_REQUIRE(smem <= dev.smem_optin, PMA_ERR_ARGUMENT, "pma_edt_noalloc: X extent too large");
-        PMA_CUDA(cudaFuncSetAttribute(edt_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
         const size_t cols = static_cast<size_t>(SY) * SZ;
         edt_pass_x<<<div_up(cols, threads), threads, smem, s>>>(solid, edt2, SX, SY, SZ, words);
         PMA_CUDA(cudaGetLastError());
@@ -341,8 +354,6 @@ void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats
         while (warps > 1 && static_cast<size_t>(warps) * SY * 4 > 96 * 1024) warps >>= 1;
         const size_t smem = static_cast<size_t>(warps) * SY * 4;
         PMA_REQUIRE(smem <= dev.smem_optin, PMA_ERR_ARGUMENT, "pma_edt_noalloc: Y extent too large");
-        PMA_CUDA(cudaFuncSetAttribute(edt_pass_y, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
         const size_t rows = static_cast<size_t>(SX) * SZ;
         const size_t blocks = std::min<size_t>((rows + warps - 1) / warps, static_cast<size_t>(dev.num_sms) * 64);
         edt_pass_y<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(edt2, SY, rows);
@@ -355,8 +366,6 @@ void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats
     {
         const size_t smem = static_cast<size_t>(SZ) * kTileY * 4 + kHistSmall * 4;
         PMA_REQUIRE(smem <= dev.smem_optin, PMA_ERR_ARGUMENT, "pma_edt_noalloc: Z extent too large");
-        PMA_CUDA(cudaFuncSetAttribute(edt_pass_z, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
         const size_t tiles = static_cast<size_t>(SX) * ((SY + kTileY - 1) / kTileY);
         edt_pass_z<<<static_cast<unsigned>(tiles), 256, smem, s>>>(edt2, SX, SY, SZ, d_hist, hist_len, d_max);
         PMA_CUDA(cudaGetLastError());

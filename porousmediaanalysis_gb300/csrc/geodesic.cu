@@ -48,7 +48,7 @@ struct Geo {
 };
 
 struct Frontier {
-    uint32_t* list[4];
+    uint32_t* lists;       // four bucket lists of cap entries each: bucket b uses list b & 3
     unsigned int* count;   // [4]
     uint32_t cap;
     unsigned int* overflow;
@@ -75,7 +75,7 @@ __device__ __forceinline__ void enqueue(const Frontier& f, int* mark, uint32_t v
     const int b = Bits<T>::bucket(d);
     if (atomicMin(&mark[v], b) <= b) return;
     const unsigned pos = atomicAdd(&f.count[b & 3], 1u);
-    if (pos < f.cap) f.list[b & 3][pos] = v;
+    if (pos < f.cap) f.lists[static_cast<size_t>(b & 3) * f.cap + pos] = v;
     else atomicExch(f.overflow, 1u);
 }
 
@@ -85,7 +85,12 @@ __global__ void geo_start(Frontier f, int* mark, T* dist, uint32_t v) {
     enqueue<T>(f, mark, v, static_cast<T>(0));
 }
 
-// Processes bucket k: settle its voxels and relax their neighbours.
+// Processes bucket k: settle its voxels and relax their neighbours. One thread per
+// (entry, stencil position): the wavefront of a bucket is a thin shell of a few thousand to a
+// few hundred thousand voxels, and 27 threads per voxel keep enough loads in flight to hide
+// their latency; the neighbours of one voxel fall in one warp and share cache lines.
+// The mark makes every voxel appear at most once in a bucket's list, so a live entry
+// (bucket(dist) == k) is settled exactly once, by its centre thread.
 template <class T>
 __global__ void geo_bucket(const uint8_t* __restrict__ solid, Geo g, int d3q7, T w1, T w2, T w3,
                            T* __restrict__ dist, uint32_t* __restrict__ cavity, int* __restrict__ mark,
@@ -93,47 +98,78 @@ __global__ void geo_bucket(const uint8_t* __restrict__ solid, Geo g, int d3q7, T
     typedef typename Bits<T>::U U;
     if (blockIdx.x == 0 && threadIdx.x == 0) f.count[(k + 3) & 3] = 0;  // list of bucket k-1
     const unsigned n = min(f.count[k & 3], f.cap);
-    const uint32_t* list = f.list[k & 3];
+    const uint32_t* list = f.lists + static_cast<size_t>(k & 3) * f.cap;
     unsigned long long my_settled = 0;
     unsigned my_walls = 0;
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long total = static_cast<unsigned long long>(n) * 27;
+    const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+    for (unsigned long long t = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const unsigned i = static_cast<unsigned>(t / 27);
+        const int j = static_cast<int>(t - static_cast<unsigned long long>(i) * 27);
         const uint32_t v = list[i];
         const T dv = dist[v];
-        if (Bits<T>::bucket(dv) != k) continue;  // stale entry
-        if (cavity[v] == cavity_id) continue;                                  // duplicate
-        cavity[v] = cavity_id;
-        ++my_settled;
-        const int y = static_cast<int>(v % g.SY);
-        const uint32_t zx = v / g.SY;
-        const int x = static_cast<int>(zx % g.SX);
-        const int z = static_cast<int>(zx / g.SX);
-        if (x == 0) my_walls |= 1u;
-        if (x == g.SX - 1 && g.SX > 1) my_walls |= 2u;
-        if (y == 0) my_walls |= 4u;
-        if (y == g.SY - 1 && g.SY > 1) my_walls |= 8u;
-        if (z == 0) my_walls |= 16u;
-        if (z == g.SZ - 1 && g.SZ > 1) my_walls |= 32u;
-        for (int dx = -1; dx <= 1; ++dx) {
-            const int nx = x + dx;
-            if (nx < 0 || nx >= g.SX) continue;
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int ny = y + dy;
-                if (ny < 0 || ny >= g.SY) continue;
-                for (int dz = -1; dz <= 1; ++dz) {
-                    const int nz = z + dz;
-                    if (nz < 0 || nz >= g.SZ) continue;
-                    const int kk = dx * dx + dy * dy + dz * dz;
-                    if (kk == 0) continue;
-                    if (d3q7 && kk > 1) continue;
-                    const size_t w = g.idx(nx, ny, nz);
-                    if (solid[w] != 0) continue;
+        bool push = false;
+        int pb = 0;
+        size_t w = 0;
+        if (Bits<T>::bucket(dv) == k) {  // else a stale entry: the voxel moved to a lower bucket
+            const int y = static_cast<int>(v % g.SY);
+            const uint32_t zx = v / g.SY;
+            const int x = static_cast<int>(zx % g.SX);
+            const int z = static_cast<int>(zx / g.SX);
+            if (j == 13) {  // centre: settle
+                cavity[v] = cavity_id;
+                ++my_settled;
+                if (x == 0) my_walls |= 1u;
+                if (x == g.SX - 1 && g.SX > 1) my_walls |= 2u;
+                if (y == 0) my_walls |= 4u;
+                if (y == g.SY - 1 && g.SY > 1) my_walls |= 8u;
+                if (z == 0) my_walls |= 16u;
+                if (z == g.SZ - 1 && g.SZ > 1) my_walls |= 32u;
+            } else {
+                const int dx = j / 9 - 1, dy = (j / 3) % 3 - 1, dz = j % 3 - 1;
+                const int kk = dx * dx + dy * dy + dz * dz;
+                const int nx = x + dx, ny = y + dy, nz = z + dz;
+                if ((!d3q7 || kk == 1) && nx >= 0 && nx < g.SX && ny >= 0 && ny < g.SY && nz >= 0 &&
+                    nz < g.SZ) {
+                    w = g.idx(nx, ny, nz);
+                    // solid voxels hold -1 and never take the (positive) new distance, so the
+                    // distance alone decides; no separate read of the solid mask
                     const T step = d3q7 ? static_cast<T>(1) : (kk == 1 ? w1 : (kk == 2 ? w2 : w3));
                     const T nd = Bits<T>::add(dv, step);
-                    if (!(nd < dist[w])) continue;
-                    const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
-                    if (Bits<T>::to(nd) < old) enqueue<T>(f, mark, static_cast<uint32_t>(w), nd);
+                    if (nd < dist[w]) {
+                        const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
+                        if (Bits<T>::to(nd) < old) {
+                            // a voxel's bucket only decreases; the mark keeps the lowest bucket
+                            // it was appended to, so each list holds it at most once
+                            pb = Bits<T>::bucket(nd);
+                            push = atomicMin(&mark[w], pb) > pb;
+                        }
+                    }
                 }
             }
+        }
+        // Appends, one counter update per warp and target list: relaxations from bucket k
+        // reach buckets k + 1 and k + 2 only (steps are in [1, 2)).
+        const unsigned active = __activemask();
+        for (int tb = 1; tb <= 2; ++tb) {
+            const bool mine = push && pb == k + tb;
+            const unsigned m = __ballot_sync(active, mine);
+            if (!m) continue;
+            const int leader = __ffs(m) - 1;
+            unsigned base = 0;
+            if (static_cast<int>(lane) == leader) base = atomicAdd(&f.count[(k + tb) & 3], static_cast<unsigned>(__popc(m)));
+            base = __shfl_sync(active, base, leader);
+            if (mine) {
+                const unsigned pos = base + __popc(m & lt);
+                if (pos < f.cap) f.lists[static_cast<size_t>((k + tb) & 3) * f.cap + pos] = static_cast<uint32_t>(w);
+                else atomicExch(f.overflow, 1u);
+            }
+        }
+        if (push && (pb < k + 1 || pb > k + 2)) {  // not reachable with steps in [1, 2)
+            const unsigned pos = atomicAdd(&f.count[pb & 3], 1u);
+            if (pos < f.cap) f.lists[static_cast<size_t>(pb & 3) * f.cap + pos] = static_cast<uint32_t>(w);
+            else atomicExch(f.overflow, 1u);
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -203,7 +239,7 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
     auto* lists = static_cast<uint32_t*>(ctx->scratch("geo.lists", 4ull * cap * 4));
     auto* misc = static_cast<unsigned long long*>(ctx->scratch("geo.misc", 64));
     Frontier f;
-    for (int i = 0; i < 4; ++i) f.list[i] = lists + static_cast<size_t>(i) * cap;
+    f.lists = lists;
     f.count = reinterpret_cast<unsigned int*>(misc);          // 4 x u32 = misc[0..1]
     f.overflow = reinterpret_cast<unsigned int*>(misc + 2);   // misc[2] low
     f.walls = reinterpret_cast<unsigned int*>(misc + 3);      // misc[3] low

@@ -78,8 +78,10 @@ struct pma_ctx {
         cudaEvent_t start, stop;
     };
     std::vector<Timed> timed;
+    std::vector<pma_ctx*> lanes;  // child contexts of batch calls (own stream and scratch)
 
     void* scratch(const std::string& tag, size_t bytes);
+    void release(const std::string& tag);  // frees one scratch buffer (after the stream's work)
     void* host_staging(size_t bytes);
     void sync();
     void check_launch(const char* what);
@@ -137,5 +139,12 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
 void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d);
 pma_table* watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* crad2, pma_dims d,
                      pma_stencil st, uint32_t max_edt2, uint32_t* labels);
+
+// Whole chain of one volume on ctx's stream (pipeline.cpp): from host buffers, or on device
+// buffers (output field pointers of `out` are device pointers, NULL = context scratch).
+void run_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims, const pma_options& o,
+                       pma_outputs* out);
+void run_pipeline_device(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, const pma_options& o,
+                         pma_outputs* out);
 
 }  // namespace pma

@@ -28,6 +28,8 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "devutil.cuh"
@@ -182,38 +184,52 @@ __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* 
                               Grid g, size_t n, int d3q7, unsigned long long* __restrict__ count,
                               unsigned long long* __restrict__ edges, unsigned long long cap) {
     unsigned long long local = 0;
-    PMA_GRID_STRIDE(v, n) {
-        const uint32_t p = pid[v];
-        if (p == kNone) continue;
-        const uint32_t r = crad[v];
-        int x, y, z;
-        g.coords(v, x, y, z);
+    const unsigned lane = threadIdx.x & 31;
+    // block-uniform trip count, so whole warps reach the warp-wide placement below
+    for (size_t base = static_cast<size_t>(blockIdx.x) * blockDim.x; base < n;
+         base += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t v = base + threadIdx.x;
         uint32_t seen[26];
         int ns = 0;
-        for (int j = 0; j < 27; ++j) {
-            int dx, dy, dz;
-            if (!stencil_offset(j, d3q7, dx, dy, dz)) continue;
-            const int nx = x + dx, ny = y + dy, nz = z + dz;
-            if (!g.inside(nx, ny, nz)) continue;
-            const size_t w = g.idx(nx, ny, nz);
-            const uint32_t rw = crad[w];
-            if (rw == 0 || rw >= r) continue;
-            const uint32_t q = pid[w];
-            bool dup = false;
-            for (int i = 0; i < ns; ++i) dup |= seen[i] == q;
-            if (dup) continue;
-            seen[ns++] = q;
-            if (kWrite) {
-                const unsigned long long pos = atomicAdd(count, 1ull);
-                if (pos < cap) edges[pos] = (static_cast<unsigned long long>(q) << 32) | p;
-            } else {
-                ++local;
+        const uint32_t p = v < n ? pid[v] : kNone;
+        if (p != kNone) {
+            const uint32_t r = crad[v];
+            int x, y, z;
+            g.coords(v, x, y, z);
+            for (int j = 0; j < 27; ++j) {
+                int dx, dy, dz;
+                if (!stencil_offset(j, d3q7, dx, dy, dz)) continue;
+                const int nx = x + dx, ny = y + dy, nz = z + dz;
+                if (!g.inside(nx, ny, nz)) continue;
+                const size_t w = g.idx(nx, ny, nz);
+                const uint32_t rw = crad[w];
+                if (rw == 0 || rw >= r) continue;
+                const uint32_t q = pid[w];
+                bool dup = false;
+                for (int i = 0; i < ns; ++i) dup |= seen[i] == q;
+                if (dup) continue;
+                seen[ns++] = q;
             }
+        }
+        if (kWrite) {
+            // one atomic per warp; lanes place their edges by a warp prefix sum
+            unsigned incl = static_cast<unsigned>(ns);
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= static_cast<unsigned>(o)) incl += t;
+            }
+            unsigned long long pos = 0;
+            if (lane == 31 && incl) pos = atomicAdd(count, static_cast<unsigned long long>(incl));
+            pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + (incl - static_cast<unsigned>(ns));
+            for (int i = 0; i < ns; ++i)
+                if (pos + i < cap) edges[pos + i] = (static_cast<unsigned long long>(seen[i]) << 32) | p;
+        } else {
+            local += ns;
         }
     }
     if (!kWrite) {
         for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
-        if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+        if (lane == 0 && local) atomicAdd(count, local);
     }
 }
 
@@ -235,9 +251,16 @@ __global__ void level_keys(const uint32_t* __restrict__ pcrad, size_t np, uint32
     }
 }
 
+constexpr int kSmallSet = 32;            // sets this small are merged by one warp
+constexpr unsigned kHeavyDegree = 1024;  // plateaus with more in-edges are reduced by a block
+constexpr int kLevelWarps = 4;           // warps per block of the per-plateau kernels
+
+// Level sweep state. Plateaus of one level are addressed by their local index L (position
+// in `order` minus the level's first position).
 struct PlateauSets {
     const unsigned int* eoff;
     const unsigned long long* edges;  // sorted by destination; low word = source
+    const uint32_t* order;            // plateaus in decreasing crad
     const uint32_t* minrank;
     uint32_t* m;       // smallest ball rank reaching the plateau
     uint32_t* seed;    // rank of the plateau's seed or kNone
@@ -246,70 +269,277 @@ struct PlateauSets {
     uint32_t* pool;
     unsigned long long pool_cap;
     unsigned int* err;
+    unsigned long long* cnt;     // [L] set size
+    unsigned long long* off;     // [L] exclusive scan of cnt
+    unsigned long long* first;   // [L] first merged element of a large set
+    uint8_t* big;                // [L] 1: merged by the sort path
+    uint32_t* heavy;             // local indices of high in-degree plateaus
+    uint32_t* big_list;          // local indices of the sort-path plateaus
+    unsigned long long* info;    // [0] heavy, [1] big, [2] big elements, [3] expansion fill
 };
 
-// First element of sorted a[0..n) greater than `last` (kNone if none).
-__device__ __forceinline__ uint32_t next_above(const uint32_t* a, uint32_t n, long long last) {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (static_cast<long long>(a[mid]) > last) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo < n ? a[lo] : kNone;
+__device__ __forceinline__ uint32_t warp_min_u32(uint32_t v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
 }
 
-// One plateau of the current level. kWrite = false: seeds, m and |S|; true: write S.
-template <bool kWrite>
-__global__ void level_sets(PlateauSets st, const uint32_t* __restrict__ order, size_t begin,
-                           size_t end, unsigned long long* __restrict__ cnt,
-                           const unsigned long long* __restrict__ off,
-                           const unsigned long long* __restrict__ base) {
-    for (size_t i = begin + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < end;
-         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const uint32_t p = order[i];
-        const unsigned int e0 = st.eoff[p], e1 = st.eoff[p + 1];
-        uint32_t seed = kNone;
-        if (!kWrite) {
-            uint32_t mp = kNone;
-            for (unsigned int e = e0; e < e1; ++e) {
-                const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-                mp = min(mp, st.m[q]);
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// Union of the predecessors' sets and the own seed when it has at most kSmallSet elements
+// (the caller checked the sum of the sizes). On return the warp holds the union sorted
+// ascending: lanes with keep = true hold element `rank`; the return value is its size.
+__device__ __forceinline__ int warp_small_union(const PlateauSets& st, unsigned e0, unsigned e1,
+                                                uint32_t seed, uint32_t* wbuf, unsigned int* wfill,
+                                                unsigned lane, uint32_t& value, bool& keep, int& rank) {
+    if (lane == 0) *wfill = 0;
+    __syncwarp();
+    for (unsigned e = e0 + lane; e < e1; e += 32) {
+        const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+        const uint32_t len = st.slen[q];
+        if (!len) continue;
+        const unsigned pos = atomicAdd(wfill, len);
+        const uint32_t* src = st.pool + st.soff[q];
+        for (uint32_t k = 0; k < len; ++k)
+            if (pos + k < kSmallSet) wbuf[pos + k] = src[k];
+    }
+    __syncwarp();
+    const unsigned total = min(*wfill, static_cast<unsigned>(kSmallSet));
+    __syncwarp();
+    uint32_t v = lane < total ? wbuf[lane] : kNone;
+    if (seed != kNone && lane == total) v = seed;
+    // bitonic sort of the 32 lanes, ascending (kNone pads sort last)
+    for (int k = 2; k <= 32; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, v, j);
+            const bool ascending = (lane & k) == 0;
+            const bool lower = (lane & j) == 0;
+            v = (lower == ascending) ? min(v, other) : max(v, other);
+        }
+    const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, v, 1);
+    keep = v != kNone && (lane == 0 || prev != v);
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, keep);
+    rank = __popc(mask & ((1u << lane) - 1u));
+    value = v;
+    return __popc(mask);
+}
+
+// Seeds, m and set sizes of one level, one warp per plateau. Small unions are counted here;
+// larger ones go to the sort path and plateaus with many in-edges to level_heavy.
+__global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
+    __shared__ uint32_t wbuf[kLevelWarps][kSmallSet];
+    __shared__ unsigned int wfill[kLevelWarps];
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t stride = static_cast<size_t>(gridDim.x) * kLevelWarps;
+    for (size_t i = begin + static_cast<size_t>(blockIdx.x) * kLevelWarps + w; i < end; i += stride) {
+        const size_t L = i - begin;
+        const uint32_t p = st.order[i];
+        const unsigned e0 = st.eoff[p], e1 = st.eoff[p + 1];
+        if (e1 - e0 > kHeavyDegree) {
+            if (lane == 0) {
+                st.big[L] = 1;
+                st.cnt[L] = 0;
+                st.heavy[atomicAdd(&st.info[0], 1ull)] = static_cast<uint32_t>(L);
             }
-            const uint32_t own = st.minrank[p];
-            if (own < mp) seed = own;
+            continue;
+        }
+        uint32_t mp = kNone;
+        unsigned long long u = 0;
+        for (unsigned e = e0 + lane; e < e1; e += 32) {
+            const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+            mp = min(mp, st.m[q]);
+            u += st.slen[q];
+        }
+        mp = warp_min_u32(mp);
+        u = warp_sum_u64(u);
+        const uint32_t own = st.minrank[p];
+        const uint32_t seed = own < mp ? own : kNone;
+        if (lane == 0) {
             st.m[p] = min(own, mp);
             st.seed[p] = seed;
-        } else {
-            seed = st.seed[p];
         }
-        long long last = -1;
-        unsigned long long k = 0;
-        unsigned long long pos = kWrite ? (*base + off[i - begin]) : 0;
-        while (true) {
-            uint32_t best = (seed != kNone && static_cast<long long>(seed) > last) ? seed : kNone;
-            for (unsigned int e = e0; e < e1; ++e) {
-                const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-                const uint32_t c = next_above(st.pool + st.soff[q], st.slen[q], last);
-                best = min(best, c);
+        const unsigned long long total = u + (seed != kNone ? 1u : 0u);
+        if (total <= kSmallSet) {
+            uint32_t v;
+            bool keep;
+            int rank;
+            const int k = warp_small_union(st, e0, e1, seed, wbuf[w], &wfill[w], lane, v, keep, rank);
+            if (lane == 0) {
+                st.big[L] = 0;
+                st.cnt[L] = static_cast<unsigned long long>(k);
             }
-            if (best == kNone) break;
-            if (kWrite) {
-                if (pos + k < st.pool_cap) st.pool[pos + k] = best;
-                else atomicOr(st.err, 2u);
-            }
-            ++k;
-            last = best;
+        } else if (lane == 0) {
+            st.big[L] = 1;
+            st.cnt[L] = 0;
+            st.big_list[atomicAdd(&st.info[1], 1ull)] = static_cast<uint32_t>(L);
+            atomicAdd(&st.info[2], total);
         }
-        if (kWrite) {
-            // A list that did not fit is recorded empty so later levels never read past the
-            // pool; the overflow flag makes the host redo the sweep with a larger pool.
-            const bool fits = pos + k <= st.pool_cap;
+    }
+}
+
+// Seeds and m of the high in-degree plateaus, one block each; they all take the sort path.
+__global__ void level_heavy(PlateauSets st, size_t begin) {
+    __shared__ uint32_t smin[32];
+    __shared__ unsigned long long ssum[32];
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned long long nh = st.info[0];
+    for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint32_t L = st.heavy[h];
+        const uint32_t p = st.order[begin + L];
+        const unsigned e0 = st.eoff[p], e1 = st.eoff[p + 1];
+        uint32_t mp = kNone;
+        unsigned long long u = 0;
+        for (unsigned e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+            mp = min(mp, st.m[q]);
+            u += st.slen[q];
+        }
+        mp = warp_min_u32(mp);
+        u = warp_sum_u64(u);
+        if (lane == 0) {
+            smin[w] = mp;
+            ssum[w] = u;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (unsigned k = 1; k < nw; ++k) {
+                mp = min(mp, smin[k]);
+                u += ssum[k];
+            }
+            const uint32_t own = st.minrank[p];
+            const uint32_t seed = own < mp ? own : kNone;
+            st.m[p] = min(own, mp);
+            st.seed[p] = seed;
+            st.big_list[atomicAdd(&st.info[1], 1ull)] = L;
+            atomicAdd(&st.info[2], u + (seed != kNone ? 1u : 0u));
+        }
+        __syncthreads();
+    }
+}
+
+// Sort path: every element of every predecessor set (and the own seed) of the big plateaus
+// becomes a key (plateau << shift | rank); sorting and removing duplicates yields each union.
+// Keys are 32-bit, with the plateau given by its index in the level's big list, whenever
+// ranks and big-list indices fit together; otherwise 64-bit with the level-local index.
+template <class K>
+__device__ __forceinline__ uint32_t key_plateau(const PlateauSets& st, K key, int shift) {
+    const uint32_t hi = static_cast<uint32_t>(key >> shift);
+    return sizeof(K) == 4 ? st.big_list[hi] : hi;
+}
+
+// In-degrees of the big plateaus (their edges are spread over the whole grid below).
+__global__ void level_big_degrees(PlateauSets st, size_t begin, unsigned long long* __restrict__ deg) {
+    const unsigned long long nbig = st.info[1];
+    PMA_GRID_STRIDE(b, nbig) {
+        const uint32_t p = st.order[begin + st.big_list[b]];
+        deg[b] = st.eoff[p + 1] - st.eoff[p];
+    }
+}
+
+// One thread per in-edge of a big plateau (t over the concatenated edge lists, doff = the
+// exclusive scan of the in-degrees): a giant plateau with a million in-edges is spread over
+// the whole GPU instead of one block. Keys of a warp are placed with one atomic.
+template <class K>
+__global__ void level_expand(PlateauSets st, size_t begin, const unsigned long long* __restrict__ doff,
+                             const unsigned long long* __restrict__ deg, unsigned long long nbig,
+                             K* __restrict__ keys, unsigned long long cap, int shift) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned long long total = doff[nbig - 1] + deg[nbig - 1];
+    const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    // warp-uniform trip count
+    for (unsigned long long t0 = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + (threadIdx.x & ~31u);
+         t0 < total; t0 += stride) {
+        const unsigned long long t = t0 + lane;
+        uint32_t len = 0;
+        const uint32_t* src = st.pool;
+        K hi = 0;
+        if (t < total) {
+            unsigned long long lo = 0, up = nbig;  // last b with doff[b] <= t
+            while (up - lo > 1) {
+                const unsigned long long mid = (lo + up) >> 1;
+                if (doff[mid] <= t) lo = mid;
+                else up = mid;
+            }
+            const uint32_t L = st.big_list[lo];
+            const uint32_t p = st.order[begin + L];
+            const uint32_t q = static_cast<uint32_t>(st.edges[st.eoff[p] + (t - doff[lo])]);
+            len = st.slen[q];
+            src = st.pool + st.soff[q];
+            hi = static_cast<K>(sizeof(K) == 4 ? lo : L) << shift;
+        }
+        unsigned long long incl = len;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<unsigned>(o)) incl += v;
+        }
+        unsigned long long pos = 0;
+        if (lane == 31 && incl) pos = atomicAdd(&st.info[3], incl);
+        pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + incl - len;
+        for (uint32_t k = 0; k < len; ++k)
+            if (pos + k < cap) keys[pos + k] = hi | static_cast<K>(src[k]);
+    }
+    // own seeds
+    for (unsigned long long b = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; b < nbig;
+         b += stride) {
+        const uint32_t L = st.big_list[b];
+        const uint32_t p = st.order[begin + L];
+        if (st.seed[p] == kNone) continue;
+        const unsigned long long pos = atomicAdd(&st.info[3], 1ull);
+        if (pos < cap) keys[pos] = (static_cast<K>(sizeof(K) == 4 ? b : L) << shift) | static_cast<K>(st.seed[p]);
+    }
+}
+
+// Sizes and first positions of the merged unions (keys sorted, duplicates removed).
+template <class K>
+__global__ void level_runs(const K* __restrict__ keys, size_t n, PlateauSets st, int shift) {
+    PMA_GRID_STRIDE(i, n) {
+        const K hi = keys[i] >> shift;
+        const uint32_t L = key_plateau(st, keys[i], shift);
+        if (i == 0 || (keys[i - 1] >> shift) != hi) st.first[L] = i;
+        atomicAdd(&st.cnt[L], 1ull);
+    }
+}
+
+// Writes the small unions (recomputed) and the list offsets of all plateaus of the level.
+__global__ void level_write(PlateauSets st, size_t begin, size_t end, const unsigned long long* __restrict__ base) {
+    __shared__ uint32_t wbuf[kLevelWarps][kSmallSet];
+    __shared__ unsigned int wfill[kLevelWarps];
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const size_t stride = static_cast<size_t>(gridDim.x) * kLevelWarps;
+    const unsigned long long b0 = *base;
+    for (size_t i = begin + static_cast<size_t>(blockIdx.x) * kLevelWarps + w; i < end; i += stride) {
+        const size_t L = i - begin;
+        const uint32_t p = st.order[i];
+        const unsigned long long pos = b0 + st.off[L], k = st.cnt[L];
+        // A list that does not fit is recorded empty so later levels never read past the
+        // pool; the overflow flag makes the host redo the sweep with a larger pool.
+        const bool fits = pos + k <= st.pool_cap;
+        if (lane == 0) {
             st.soff[p] = fits ? pos : 0;
             st.slen[p] = fits ? static_cast<uint32_t>(k) : 0u;
-        } else {
-            cnt[i - begin] = k;
+            if (!fits) atomicOr(st.err, 2u);
         }
+        if (st.big[L]) continue;
+        uint32_t v;
+        bool keep;
+        int rank;
+        warp_small_union(st, st.eoff[p], st.eoff[p + 1], st.seed[p], wbuf[w], &wfill[w], lane, v, keep, rank);
+        if (keep && fits) st.pool[pos + rank] = v;
+    }
+}
+
+template <class K>
+__global__ void level_copy_big(const K* __restrict__ keys, size_t n, PlateauSets st,
+                               const unsigned long long* __restrict__ base, int shift) {
+    const unsigned long long b0 = *base;
+    const K low = (static_cast<K>(1) << shift) - 1;
+    PMA_GRID_STRIDE(i, n) {
+        const uint32_t L = key_plateau(st, keys[i], shift);
+        const unsigned long long pos = b0 + st.off[L];
+        if (pos + st.cnt[L] <= st.pool_cap)
+            st.pool[pos + (i - st.first[L])] = static_cast<uint32_t>(keys[i] & low);
     }
 }
 
@@ -445,15 +675,6 @@ __global__ void gather_lists(const unsigned long long* __restrict__ soff, const 
     }
 }
 
-struct MaxBall {  // same layout as the reference's Model::MaximumBall (Types.h:182-186)
-    int center[3];
-    uint32_t r2;
-};
-
-struct MaxBallDescending {  // Types.h:188-195
-    bool operator()(const MaxBall& a, const MaxBall& b) const { return a.r2 > b.r2; }
-};
-
 template <class T>
 T* buf(pma_ctx* ctx, const char* tag, size_t count) {
     return static_cast<T*>(ctx->scratch(tag, std::max<size_t>(count, 1) * sizeof(T)));
@@ -492,28 +713,23 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemcpyAsync(h_r2.data(), ball_r2, nb * 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
     }
-    // std::sort with the reference's comparator (PoreAndThroatComputer.cpp:121-122).
-    std::vector<MaxBall> mb(nb);
-    for (int64_t i = 0; i < nb; ++i) {
-        int x, y, z;
-        g.coords(h_idx[i], x, y, z);
-        mb[i].center[0] = x;
-        mb[i].center[1] = y;
-        mb[i].center[2] = z;
-        mb[i].r2 = h_r2[i];
-    }
-    std::sort(mb.begin(), mb.end(), MaxBallDescending());
-    std::vector<uint32_t> voxel_of_rank(nb);
-    for (int64_t r = 0; r < nb; ++r)
-        voxel_of_rank[r] = static_cast<uint32_t>(g.idx(mb[r].center[0], mb[r].center[1], mb[r].center[2]));
-    uint32_t* crank = buf<uint32_t>(ctx, "pores.crank", n);
-    fill_u32<<<G, 256, 0, s>>>(crank, n, kNone);
-    ctx->check_launch("fill_u32");
-    if (nb) {
-        PMA_CUDA(cudaMemcpyAsync(balls, voxel_of_rank.data(), nb * 4, cudaMemcpyHostToDevice, s));
-        scatter_rank<<<grid_for(ctx, nb), 256, 0, s>>>(balls, nb, crank);
-        ctx->check_launch("scatter_rank");
-    }
+    // std::sort with the reference's comparator (PoreAndThroatComputer.cpp:121-122), run on a
+    // host thread while the plateau kernels below run. The items are 8-byte (r2, scan index)
+    // pairs compared on r2 alone: std::sort's moves depend only on comparison results, so
+    // the permutation equals the one the reference's 16-byte balls go through.
+    std::vector<unsigned long long> items(nb);
+    for (int64_t i = 0; i < nb; ++i)
+        items[i] = (static_cast<unsigned long long>(h_r2[i]) << 32) | static_cast<unsigned long long>(i);
+    struct Joiner {
+        std::thread t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } sorter;
+    sorter.t = std::thread([&items] {
+        std::sort(items.begin(), items.end(),
+                  [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); });
+    });
 
     // Plateaus: connected sets of equal crad under the stencil.
     uint32_t* pid = buf<uint32_t>(ctx, "pores.pid", n);  // root voxel, then plateau id
@@ -541,18 +757,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         ctx->sync();
         PMA_REQUIRE(!(h_err & 8u), PMA_ERR_INTERNAL, "pma_pores: plateau labelling left a non-root parent");
     }
-    uint32_t* pcrad = buf<uint32_t>(ctx, "pores.pcrad", np);
-    unsigned int* psize = buf<unsigned int>(ctx, "pores.psize", np);
-    unsigned int* pface = buf<unsigned int>(ctx, "pores.pface", np);
-    uint32_t* pminrank = buf<uint32_t>(ctx, "pores.pminrank", np);
-    PMA_CUDA(cudaMemsetAsync(psize, 0, std::max<int64_t>(np, 1) * 4, s));
-    PMA_CUDA(cudaMemsetAsync(pface, 0, std::max<int64_t>(np, 1) * 4, s));
-    fill_u32<<<grid_for(ctx, np), 256, 0, s>>>(pminrank, np, kNone);
-    ctx->check_launch("fill_u32");
-    plateau_stats<<<G, 256, 0, s>>>(pid, crad2, crank, g, n, pcrad, psize, pface, pminrank);
-    ctx->check_launch("plateau_stats");
-
     // Edges between plateaus, sorted by destination.
+    auto kt_edges = std::make_unique<KernelTimer>(ctx, "plateau_edges");
     auto* ecount = reinterpret_cast<unsigned long long*>(d_count + 1);
     PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
     plateau_edges<false><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, nullptr, 0);
@@ -576,6 +782,33 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     PMA_CUDA(cudaMemsetAsync(eoff, 0, (np + 1) * 4, s));
     edge_offsets<<<grid_for(ctx, ne + 1), 256, 0, s>>>(by_dst, ne, np, eoff);
     ctx->check_launch("edge_offsets");
+    kt_edges.reset();
+
+    auto kt_join = std::make_unique<KernelTimer>(ctx, "pores_sort_wait");
+    sorter.t.join();
+    kt_join.reset();
+    auto kt_stats = std::make_unique<KernelTimer>(ctx, "plateau_stats");
+    std::vector<uint32_t> voxel_of_rank(nb);
+    for (int64_t r = 0; r < nb; ++r) voxel_of_rank[r] = h_idx[items[r] & 0xFFFFFFFFull];
+    uint32_t* crank = buf<uint32_t>(ctx, "pores.crank", n);
+    fill_u32<<<G, 256, 0, s>>>(crank, n, kNone);
+    ctx->check_launch("fill_u32");
+    if (nb) {
+        PMA_CUDA(cudaMemcpyAsync(balls, voxel_of_rank.data(), nb * 4, cudaMemcpyHostToDevice, s));
+        scatter_rank<<<grid_for(ctx, nb), 256, 0, s>>>(balls, nb, crank);
+        ctx->check_launch("scatter_rank");
+    }
+    uint32_t* pcrad = buf<uint32_t>(ctx, "pores.pcrad", np);
+    unsigned int* psize = buf<unsigned int>(ctx, "pores.psize", np);
+    unsigned int* pface = buf<unsigned int>(ctx, "pores.pface", np);
+    uint32_t* pminrank = buf<uint32_t>(ctx, "pores.pminrank", np);
+    PMA_CUDA(cudaMemsetAsync(psize, 0, std::max<int64_t>(np, 1) * 4, s));
+    PMA_CUDA(cudaMemsetAsync(pface, 0, std::max<int64_t>(np, 1) * 4, s));
+    fill_u32<<<grid_for(ctx, np), 256, 0, s>>>(pminrank, np, kNone);
+    ctx->check_launch("fill_u32");
+    plateau_stats<<<G, 256, 0, s>>>(pid, crad2, crank, g, n, pcrad, psize, pface, pminrank);
+    ctx->check_launch("plateau_stats");
+    kt_stats.reset();
 
     // Levels: plateaus in decreasing crad.
     uint32_t* lkey = buf<uint32_t>(ctx, "pores.lkey", np);
@@ -602,16 +835,26 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     PlateauSets ps;
     ps.eoff = eoff;
     ps.edges = by_dst;
+    ps.order = order;
     ps.minrank = pminrank;
     ps.m = buf<uint32_t>(ctx, "pores.m", np);
     ps.seed = buf<uint32_t>(ctx, "pores.seed", np);
     ps.soff = buf<unsigned long long>(ctx, "pores.soff", np);
     ps.slen = buf<uint32_t>(ctx, "pores.slen", np);
     ps.err = err;
-    unsigned long long* cnt = buf<unsigned long long>(ctx, "pores.cnt", max_level);
-    unsigned long long* off = buf<unsigned long long>(ctx, "pores.off", max_level);
+    ps.cnt = buf<unsigned long long>(ctx, "pores.cnt", max_level);
+    ps.off = buf<unsigned long long>(ctx, "pores.off", max_level);
+    ps.first = buf<unsigned long long>(ctx, "pores.first", max_level);
+    ps.big = buf<uint8_t>(ctx, "pores.big", max_level);
+    ps.heavy = buf<uint32_t>(ctx, "pores.heavy", max_level);
+    ps.big_list = buf<uint32_t>(ctx, "pores.big_list", max_level);
+    ps.info = buf<unsigned long long>(ctx, "pores.info", 4);
     unsigned long long* base = reinterpret_cast<unsigned long long*>(d_count + 3);
+    auto* h_info = static_cast<unsigned long long*>(ctx->host_staging(32));
     unsigned long long pool_cap = std::max<unsigned long long>(1ull << 22, 32ull * np);
+    int rank_bits = 1;  // bits of a ball rank
+    while (rank_bits < 32 && (1ull << rank_bits) < static_cast<unsigned long long>(nb)) ++rank_bits;
+    const unsigned heavy_grid = static_cast<unsigned>(ctx->num_sms * 2);
     for (int attempt = 0; attempt < 3; ++attempt) {
         ps.pool = buf<uint32_t>(ctx, "pores.pool", pool_cap);
         ps.pool_cap = pool_cap;
@@ -620,12 +863,77 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         KernelTimer kt(ctx, "level_sets");
         for (size_t l = 0; l + 1 < level_begin.size(); ++l) {
             const size_t b = level_begin[l], e = level_begin[l + 1];
-            const unsigned lg = grid_for(ctx, e - b, 128);
-            level_sets<false><<<lg, 128, 0, s>>>(ps, order, b, e, cnt, nullptr, nullptr);
-            exclusive_sum(ctx, cnt, off, static_cast<int64_t>(e - b));
-            level_sets<true><<<lg, 128, 0, s>>>(ps, order, b, e, cnt, off, base);
-            level_advance<<<1, 32, 0, s>>>(base, off, cnt, e - b);
-            ctx->count_launch(3);
+            const unsigned lg = grid_for(ctx, (e - b) * 32, kLevelWarps * 32);
+            PMA_CUDA(cudaMemsetAsync(ps.info, 0, 32, s));
+            {
+                KernelTimer kt2(ctx, "level_seeds");
+                level_seeds<<<lg, kLevelWarps * 32, 0, s>>>(ps, b, e);
+                level_heavy<<<heavy_grid, 512, 0, s>>>(ps, b);
+                ctx->count_launch(2);
+            }
+            PMA_CUDA(cudaMemcpyAsync(h_info, ps.info, 32, cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            const unsigned long long nbig = h_info[1], total = h_info[2];
+            int64_t merged = 0;
+            int shift = 32;
+            void* keys = nullptr;
+            bool narrow = false;
+            if (nbig) {
+                KernelTimer kt2(ctx, "level_merge");
+                PMA_REQUIRE(total < (1ull << 40), PMA_ERR_MEMORY, "pma_pores: seed-set union too large");
+                int big_bits = 0;
+                while ((1ull << big_bits) < nbig) ++big_bits;
+                narrow = rank_bits < 32 && rank_bits + big_bits <= 32;
+                auto* deg = buf<unsigned long long>(ctx, "pores.bdeg", nbig);
+                auto* doff = buf<unsigned long long>(ctx, "pores.bdoff", nbig);
+                level_big_degrees<<<grid_for(ctx, nbig), 256, 0, s>>>(ps, b, deg);
+                ctx->check_launch("level_big_degrees");
+                exclusive_sum(ctx, deg, doff, static_cast<int64_t>(nbig));
+                const unsigned eg = static_cast<unsigned>(ctx->num_sms * 16);
+                if (narrow) {
+                    shift = rank_bits;
+                    auto* k32 = buf<uint32_t>(ctx, "pores.lkeys32", total);
+                    auto* k32b = buf<uint32_t>(ctx, "pores.lkeys32b", total);
+                    level_expand<uint32_t><<<eg, 256, 0, s>>>(ps, b, doff, deg, nbig, k32, total, shift);
+                    ctx->check_launch("level_expand");
+                    sort_keys(ctx, k32, k32b, static_cast<int64_t>(total), rank_bits + big_bits);
+                    merged = unique(ctx, k32b, k32, static_cast<int64_t>(total), d_count);
+                    keys = k32;
+                    if (merged) {
+                        level_runs<uint32_t><<<grid_for(ctx, merged), 256, 0, s>>>(k32, merged, ps, shift);
+                        ctx->check_launch("level_runs");
+                    }
+                } else {
+                    auto* k64 = buf<unsigned long long>(ctx, "pores.lkeys", total);
+                    auto* k64b = buf<unsigned long long>(ctx, "pores.lkeys2", total);
+                    level_expand<unsigned long long><<<eg, 256, 0, s>>>(ps, b, doff, deg, nbig, k64, total, shift);
+                    ctx->check_launch("level_expand");
+                    int bits = 32;
+                    while (bits < 64 && (1ull << (bits - 32)) < e - b) ++bits;
+                    sort_keys(ctx, k64, k64b, static_cast<int64_t>(total), bits);
+                    merged = unique(ctx, k64b, k64, static_cast<int64_t>(total), d_count);
+                    keys = k64;
+                    if (merged) {
+                        level_runs<unsigned long long><<<grid_for(ctx, merged), 256, 0, s>>>(k64, merged, ps, shift);
+                        ctx->check_launch("level_runs");
+                    }
+                }
+            }
+            KernelTimer kt3(ctx, "level_write");
+            exclusive_sum(ctx, ps.cnt, ps.off, static_cast<int64_t>(e - b));
+            level_write<<<lg, kLevelWarps * 32, 0, s>>>(ps, b, e, base);
+            ctx->count_launch(1);
+            if (merged) {
+                if (narrow)
+                    level_copy_big<uint32_t><<<grid_for(ctx, merged), 256, 0, s>>>(
+                        static_cast<uint32_t*>(keys), merged, ps, base, shift);
+                else
+                    level_copy_big<unsigned long long><<<grid_for(ctx, merged), 256, 0, s>>>(
+                        static_cast<unsigned long long*>(keys), merged, ps, base, shift);
+                ctx->count_launch(1);
+            }
+            level_advance<<<1, 32, 0, s>>>(base, ps.off, ps.cnt, e - b);
+            ctx->count_launch(1);
         }
         ctx->check_launch("level_sets");
         unsigned int h_err = 0;
@@ -640,6 +948,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     }
 
     // Seeds -> pores in rank order.
+    KernelTimer kt_tables(ctx, "pores_tables");
     std::vector<uint32_t> h_seed(np);
     if (np) PMA_CUDA(cudaMemcpyAsync(h_seed.data(), ps.seed, np * 4, cudaMemcpyDeviceToHost, s));
     ctx->sync();
@@ -684,7 +993,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     pma_table* t = new pma_table;
     std::vector<unsigned long long> h_gvol, h_gfirst;
     std::vector<uint32_t> h_grep;
-    std::vector<std::vector<uint32_t>> glist;
+    std::vector<uint32_t> flat;                // seed ranks of each group's list, concatenated
+    std::vector<unsigned long long> roff(1, 0);  // list offsets into flat
     int64_t ngroups = 0;
     if (nm) {
         auto* h1 = buf<unsigned long long>(ctx, "pores.h1", nm);
@@ -740,7 +1050,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         ctx->check_launch("gather_u32");
         PMA_CUDA(cudaMemcpyAsync(rlen.data(), d_rep_len, ngroups * 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
-        std::vector<unsigned long long> roff(ngroups + 1, 0);
+        roff.assign(ngroups + 1, 0);
         for (int64_t gi = 0; gi < ngroups; ++gi) roff[gi + 1] = roff[gi] + rlen[gi];
         auto* d_roff = buf<unsigned long long>(ctx, "pores.roff", ngroups + 1);
         uint32_t* d_rlist = buf<uint32_t>(ctx, "pores.rlist", roff[ngroups]);
@@ -748,19 +1058,16 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         gather_lists<<<grid_for(ctx, ngroups), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, go.grep, d_roff,
                                                             ngroups, d_rlist);
         ctx->check_launch("gather_lists");
-        std::vector<uint32_t> flat(roff[ngroups]);
+        flat.resize(roff[ngroups]);
         PMA_CUDA(cudaMemcpyAsync(flat.data(), d_rlist, flat.size() * 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
-        glist.resize(ngroups);
-        for (int64_t gi = 0; gi < ngroups; ++gi)
-            glist[gi].assign(flat.begin() + roff[gi], flat.begin() + roff[gi + 1]);
     }
     // Throat ids: order by (last pore of the type, first voxel), counting down from
     // UINT32_MAX - 1 (BasePoreAndThroatComputer.cpp:122-130).
     std::vector<int64_t> gorder(ngroups);
     for (int64_t i = 0; i < ngroups; ++i) gorder[i] = i;
     std::sort(gorder.begin(), gorder.end(), [&](int64_t a, int64_t b) {
-        const uint32_t la = glist[a].back(), lb = glist[b].back();
+        const uint32_t la = flat[roff[a + 1] - 1], lb = flat[roff[b + 1] - 1];
         if (la != lb) return la < lb;
         return h_gfirst[a] < h_gfirst[b];
     });
@@ -788,14 +1095,16 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     }
     ctx->sync();
     for (size_t k = 0; k < npores; ++k) {
-        const MaxBall& b = mb[seed_ranks[k]];
+        const uint32_t r = seed_ranks[k];
+        int x, y, z;
+        g.coords(voxel_of_rank[r], x, y, z);
         pma_pore p;
         std::memset(&p, 0, sizeof(p));
         p.id = ids[k];
-        p.seed_x = b.center[0];
-        p.seed_y = b.center[1];
-        p.seed_z = b.center[2];
-        p.seed_r2 = b.r2;
+        p.seed_x = x;
+        p.seed_y = y;
+        p.seed_z = z;
+        p.seed_r2 = static_cast<uint32_t>(items[r] >> 32);
         p.is_boundary = pbound[k] ? 1 : 0;
         p.volume = pvol[k];
         t->pores.push_back(p);
@@ -809,11 +1118,12 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         th.id = group_tid_h[gi];
         th.volume = h_gvol[gi];
         th.pool_offset = t->pool.size();
-        const std::vector<uint32_t>& L = glist[gi];
-        th.n_pores = static_cast<uint32_t>(L.size());
+        const uint32_t* L = flat.data() + roff[gi];
+        const size_t nl = roff[gi + 1] - roff[gi];
+        th.n_pores = static_cast<uint32_t>(nl);
         t->pool.push_back(rank2id[L[1]]);
         t->pool.push_back(rank2id[L[0]]);
-        for (size_t k = 2; k < L.size(); ++k) t->pool.push_back(rank2id[L[k]]);
+        for (size_t k = 2; k < nl; ++k) t->pool.push_back(rank2id[L[k]]);
         t->throats.push_back(th);
     }
     return t;
@@ -823,7 +1133,6 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
 void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d) {
     check_dims(d);
     PMA_REQUIRE(labels, PMA_ERR_ARGUMENT, "pma_remove_empty_pores: null labels");
-    std::map<uint32_t, uint32_t> remap;
     // EPR.cpp:193-244: drop zero-volume pores and remove them from the type lists.
     std::vector<uint32_t> empty;
     std::vector<pma_pore> kept;
@@ -832,62 +1141,83 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
         else kept.push_back(p);
     }
     std::sort(empty.begin(), empty.end());
-    struct Row {
-        uint32_t id;
-        uint64_t volume;
-        std::vector<uint32_t> pores;
-    };
-    std::map<uint32_t, Row> rows;
-    for (const pma_throat& th : t->throats) {
-        Row r;
-        r.id = th.id;
-        r.volume = th.volume;
-        r.pores.assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
-        std::sort(r.pores.begin(), r.pores.end());
-        std::vector<uint32_t> k;
-        std::set_difference(r.pores.begin(), r.pores.end(), empty.begin(), empty.end(), std::back_inserter(k));
-        r.pores = k;
-        rows[r.id] = r;
+    // Types in ascending id order with sorted, filtered pore lists (flat arrays).
+    const size_t nt = t->throats.size();
+    std::vector<uint32_t> by_id(nt);
+    for (size_t i = 0; i < nt; ++i) by_id[i] = static_cast<uint32_t>(i);
+    std::sort(by_id.begin(), by_id.end(),
+              [&](uint32_t a, uint32_t b) { return t->throats[a].id < t->throats[b].id; });
+    std::vector<uint32_t> lists;
+    std::vector<size_t> loff(nt + 1, 0);
+    std::vector<uint32_t> tmp;
+    for (size_t k = 0; k < nt; ++k) {
+        const pma_throat& th = t->throats[by_id[k]];
+        tmp.assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
+        std::sort(tmp.begin(), tmp.end());
+        for (uint32_t pid : tmp)
+            if (!std::binary_search(empty.begin(), empty.end(), pid)) lists.push_back(pid);
+        loff[k + 1] = lists.size();
     }
+    auto len = [&](size_t k) { return loff[k + 1] - loff[k]; };
+    std::vector<char> alive(nt, 1);
+    std::vector<std::pair<uint32_t, uint32_t>> remap;  // (old id, new id)
     // EPR.cpp:167-191: types with fewer than two pores.
-    std::vector<uint32_t> few;
-    for (auto& kv : rows)
-        if (kv.second.pores.size() < 2) few.push_back(kv.first);
-    for (uint32_t id : few) {
-        if (rows[id].pores.size() == 1) remap[id] = rows[id].pores[0];
-        rows.erase(id);
-    }
-    // EPR.cpp:126-165: merge duplicates into the largest id.
-    std::map<std::vector<uint32_t>, std::vector<uint32_t>> by_pores;
-    for (auto& kv : rows) by_pores[kv.second.pores].push_back(kv.first);
-    for (auto& kv : by_pores) {
-        const std::vector<uint32_t>& idsv = kv.second;
-        if (idsv.size() < 2) continue;
-        const uint32_t keep = *std::max_element(idsv.begin(), idsv.end());
-        for (uint32_t id : idsv)
-            if (id != keep) {
-                rows.erase(id);
-                remap[id] = keep;
+    for (size_t k = 0; k < nt; ++k)
+        if (len(k) < 2) {
+            if (len(k) == 1) remap.emplace_back(t->throats[by_id[k]].id, lists[loff[k]]);
+            alive[k] = 0;
+        }
+    // EPR.cpp:126-165: merge types with equal pore lists into the largest id.
+    std::vector<uint32_t> live;
+    for (size_t k = 0; k < nt; ++k)
+        if (alive[k]) live.push_back(static_cast<uint32_t>(k));
+    auto less_list = [&](uint32_t a, uint32_t b) {
+        return std::lexicographical_compare(lists.begin() + loff[a], lists.begin() + loff[a + 1],
+                                            lists.begin() + loff[b], lists.begin() + loff[b + 1]);
+    };
+    auto same_list = [&](uint32_t a, uint32_t b) {
+        return len(a) == len(b) && std::equal(lists.begin() + loff[a], lists.begin() + loff[a + 1],
+                                              lists.begin() + loff[b]);
+    };
+    std::stable_sort(live.begin(), live.end(), less_list);
+    for (size_t i = 0; i < live.size();) {
+        size_t j = i + 1;
+        while (j < live.size() && same_list(live[i], live[j])) ++j;
+        if (j - i > 1) {
+            uint32_t keep = 0;
+            for (size_t q = i; q < j; ++q) keep = std::max(keep, t->throats[by_id[live[q]]].id);
+            for (size_t q = i; q < j; ++q) {
+                const uint32_t id = t->throats[by_id[live[q]]].id;
+                if (id != keep) {
+                    alive[live[q]] = 0;
+                    remap.emplace_back(id, keep);
+                }
             }
+        }
+        i = j;
+    }
+    std::vector<pma_throat> throats;
+    std::vector<uint32_t> pool;
+    for (size_t k = 0; k < nt; ++k) {
+        if (!alive[k]) continue;
+        pma_throat th;
+        th.id = t->throats[by_id[k]].id;
+        th.volume = t->throats[by_id[k]].volume;
+        th.n_pores = static_cast<uint32_t>(len(k));
+        th.pool_offset = pool.size();
+        pool.insert(pool.end(), lists.begin() + loff[k], lists.begin() + loff[k + 1]);
+        throats.push_back(th);
     }
     t->pores = kept;
-    t->throats.clear();
-    t->pool.clear();
-    for (auto& kv : rows) {
-        pma_throat th;
-        th.id = kv.first;
-        th.volume = kv.second.volume;
-        th.n_pores = static_cast<uint32_t>(kv.second.pores.size());
-        th.pool_offset = t->pool.size();
-        t->pool.insert(t->pool.end(), kv.second.pores.begin(), kv.second.pores.end());
-        t->throats.push_back(th);
-    }
+    t->throats.swap(throats);
+    t->pool.swap(pool);
+    std::sort(remap.begin(), remap.end());
     if (remap.empty()) return;  // EPR.cpp:54-57
     std::vector<uint32_t> o, nw;
     for (auto& kv : remap) {
         o.push_back(kv.first);
         nw.push_back(kv.second);
-    }
+    }  // ascending old ids: remap_labels searches them
     cudaStream_t s = ctx->stream;
     uint32_t* d_old = buf<uint32_t>(ctx, "remove.old", o.size());
     uint32_t* d_new = buf<uint32_t>(ctx, "remove.new", nw.size());

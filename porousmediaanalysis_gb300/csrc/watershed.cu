@@ -15,8 +15,9 @@
 //   claim    - the smallest-time touch of each unclaimed voxel wins (atomicMin on time);
 //   resolve  - the winner records the claim; a voxel of the same depth joins the next
 //              generation, a shallower one is appended, time-stamped, to its depth's bucket,
-//              which is sorted by time when that depth starts;
-//   extend   - touches by other pores record, per voxel and pore, their first touch time.
+//              which is sorted by time when that depth starts; in the same pass, touches by
+//              pores other than the voxel's owner record, per voxel and pore, their first
+//              touch time (extensions).
 // Frontier sizes stay on the device; the next generation is compacted in event order by a
 // count / scan / scatter over event slots stamped with the generation number.
 //
@@ -25,6 +26,7 @@
 // hashed, grouped with radix sorts and ranked by creation time on the device, which
 // reproduces the reference's id sequence (UINT32_MAX - 1, - 2, ...) exactly, including
 // types whose volume later dropped to zero.
+#include <cooperative_groups.h>
 #include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
@@ -41,14 +43,18 @@ constexpr unsigned long long kNoTime = ~0ull;
 constexpr int kSlots = 6;         // distinct extending pores recorded per shared voxel
 constexpr int kKey = kSlots + 1;  // longest key
 constexpr int kChunk = 1024;      // event slots per compaction block
-constexpr int kGensPerSync = 8;
+constexpr int kGensPerLaunch = 64;  // generations per cooperative launch (host checks between)
+constexpr unsigned long long kMaxGen = 1ull << 23;              // generations per call
+constexpr unsigned long long kSeqMask = (1ull << 40) - 1;       // touch time within a generation
+constexpr uint32_t kRecBusy = 0xFFFFFFFFu;  // ext[w] while its record is being allocated
+constexpr int kSpinLimit = 1 << 20;
 
 struct WsState {
     Grid g;
     int d3q7;
     const uint32_t* crad;
     uint32_t* claim;              // pore index + 1, 0 = unclaimed
-    unsigned long long* ckey;     // per-generation claim time (kNoTime when idle)
+    unsigned long long* ckey;     // tagged claim time of the latest generation that touched it
     uint32_t* ext;                // shared-voxel record + 1, 0 = none
     uint32_t* ext_pore;           // [records][kSlots]
     unsigned long long* ext_time;
@@ -86,41 +92,115 @@ __global__ void ws_seed_entries(const unsigned long long* __restrict__ a, size_t
     }
 }
 
-__global__ void ws_histograms(const uint32_t* __restrict__ crad, size_t n, unsigned int* __restrict__ hist) {
+// Voxel count per containing radius. Few distinct radii take most voxels, so counts gather
+// in a shared-memory copy of the bins first when they fit (nb <= kHistShared).
+constexpr uint32_t kHistShared = 8192;
+
+__global__ void ws_histograms(const uint32_t* __restrict__ crad, size_t n, uint32_t nb,
+                              unsigned int* __restrict__ hist) {
+    __shared__ unsigned int local[kHistShared];
+    const bool shared = nb <= kHistShared;
+    if (shared)
+        for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) local[i] = 0;
+    __syncthreads();
     PMA_GRID_STRIDE(v, n) {
         const uint32_t r = crad[v];
-        if (r) atomicAdd(&hist[r], 1u);
+        if (!r) continue;
+        if (shared) atomicAdd(&local[r], 1u);
+        else atomicAdd(&hist[r], 1u);
     }
+    __syncthreads();
+    if (shared)
+        for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
+            if (local[i]) atomicAdd(&hist[i], local[i]);
 }
 
-// Touch events of the generation's nodes. Phase 0 claims, 1 resolves, 2 extends.
+// Records that `pore` touched shared voxel w at time t (its first touch per pore is kept).
+// Out of line: it is the rare path of the touch kernel.
+// A voxel's record is allocated by the one touch that moves ext[w] from 0 to kRecBusy;
+// touches that meet kRecBusy wait (a few instructions) for the record number.
+__device__ __noinline__ void ws_extend(uint32_t* ext, unsigned int* ext_count, uint32_t ext_cap,
+                                       uint32_t* ext_pore, unsigned long long* ext_time, unsigned int* err,
+                                       size_t w, uint32_t pore, unsigned long long t) {
+    uint32_t rec = *reinterpret_cast<volatile uint32_t*>(ext + w);
+    if (rec == 0) {
+        rec = atomicCAS(&ext[w], 0u, kRecBusy);
+        if (rec == 0) {
+            const uint32_t fresh = atomicAdd(ext_count, 1u) + 1;
+            if (fresh > ext_cap) {  // out of records: give the number back, flag a redo
+                atomicSub(ext_count, 1u);
+                atomicExch(&ext[w], 0u);
+                atomicOr(err, 1u);
+                return;
+            }
+            atomicExch(&ext[w], fresh);
+            rec = fresh;
+        }
+    }
+    for (int spins = 0; rec == kRecBusy; ++spins) {
+        if (spins > kSpinLimit) {
+            atomicOr(err, 8u);
+            return;
+        }
+        rec = atomicAdd(&ext[w], 0u);
+    }
+    if (rec == 0) {  // the allocating touch ran out of records
+        atomicOr(err, 1u);
+        return;
+    }
+    for (int k = 0; k < kSlots; ++k) {
+        const size_t slot = static_cast<size_t>(rec - 1) * kSlots + k;
+        const uint32_t cur = atomicCAS(&ext_pore[slot], kNone, pore);
+        if (cur == kNone || cur == pore) {
+            atomicMin(&ext_time[slot], t);
+            return;
+        }
+    }
+    atomicOr(err, 2u);
+}
+
+// Touch events of the generation's nodes. Phase 0 claims: the smallest touch time of each
+// unclaimed voxel wins. Claim keys carry a generation tag that decreases from one generation
+// to the next, so a key left by an earlier generation is larger than any key of the current
+// one and ckey never needs clearing. Phase 1 resolves: the winner records its claim, and
+// every other touch by a pore other than the voxel's owner - the winner's pore for a voxel
+// claimed in this generation, else the stored claim - is an extension.
+// One thread per event (node i, stencil position j): seq = i * 27 + j.
+// All generations of a launch run in one kernel (see ws_generations), so data written by
+// other blocks earlier in the launch is read with __ldcg (L2, not a possibly stale L1 line);
+// only the radii, which never change, go through the read-only path.
 template <int kPhase>
-__global__ void ws_touch(WsState s, const uint32_t* __restrict__ gv, const uint32_t* __restrict__ gp,
-                         const unsigned int* __restrict__ d_ng, uint32_t depth, unsigned long long gen) {
-    const size_t ng = *d_ng;
-    PMA_GRID_STRIDE(i, ng) {
-        const uint32_t v = gv[i];
-        const uint32_t pore = gp[i];
+__device__ __forceinline__ void ws_touch(const WsState& s, const uint32_t* gv, const uint32_t* gp,
+                                         unsigned long long nev, uint32_t depth, unsigned long long gen,
+                                         unsigned long long tid, unsigned long long stride) {
+    const unsigned long long tag = kMaxGen - gen;
+    for (unsigned long long seq = tid; seq < nev; seq += stride) {
+        const unsigned long long i = seq / 27;
+        const int j = static_cast<int>(seq - i * 27);
+        int dx, dy, dz;
+        if (!stencil_offset(j, s.d3q7, dx, dy, dz)) continue;
+        const uint32_t v = __ldcg(gv + i);
+        const uint32_t pore = __ldcg(gp + i);
         int x, y, z;
         s.g.coords(v, x, y, z);
-        for (int j = 0; j < 27; ++j) {
-            int dx, dy, dz;
-            if (!stencil_offset(j, s.d3q7, dx, dy, dz)) continue;
-            const int nx = x + dx, ny = y + dy, nz = z + dz;
-            if (!s.g.inside(nx, ny, nz)) {  // WC.cpp:140-144
-                if (kPhase == 0) s.pbound[pore] = 1;
-                continue;
-            }
-            const size_t w = s.g.idx(nx, ny, nz);
-            const uint32_t r = s.crad[w];
-            if (r == 0 || r > depth) continue;  // WC.cpp:152-156
-            const unsigned long long seq = static_cast<unsigned long long>(i) * 27 + j;
-            if (kPhase == 0) {
-                if (s.claim[w] == 0) atomicMin(&s.ckey[w], seq);
-            } else if (kPhase == 1) {
-                if (s.ckey[w] != seq) continue;
+        const int nx = x + dx, ny = y + dy, nz = z + dz;
+        if (!s.g.inside(nx, ny, nz)) {  // WC.cpp:140-144
+            if (kPhase == 0) s.pbound[pore] = 1;
+            continue;
+        }
+        const size_t w = s.g.idx(nx, ny, nz);
+        const uint32_t r = __ldg(s.crad + w);
+        if (r == 0 || r > depth) continue;  // WC.cpp:152-156
+        if (kPhase == 0) {
+            if (__ldcg(s.claim + w) == 0) atomicMin(&s.ckey[w], (tag << 40) | seq);
+            continue;
+        }
+        const unsigned long long k = __ldcg(s.ckey + w);
+        uint32_t owner;
+        if ((k >> 40) == tag) {  // unclaimed when this generation started
+            const unsigned long long wseq = k & kSeqMask;
+            if (wseq == seq) {
                 s.claim[w] = pore + 1;
-                s.ckey[w] = kNoTime;
                 if (r == depth) {
                     s.slot_voxel[seq] = static_cast<uint32_t>(w);
                     s.slot_gen[seq] = static_cast<uint32_t>(gen);
@@ -130,71 +210,51 @@ __global__ void ws_touch(WsState s, const uint32_t* __restrict__ gv, const uint3
                     s.ent_time[at] = (gen << 40) | seq;
                     s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
                 }
-            } else {
-                if (s.claim[w] == pore + 1) continue;
-                uint32_t rec = s.ext[w];
-                if (rec == 0) {
-                    const uint32_t fresh = atomicAdd(s.ext_count, 1u) + 1;
-                    if (fresh > s.ext_cap) {
-                        atomicOr(s.err, 1u);
-                        continue;
-                    }
-                    const uint32_t old = atomicCAS(&s.ext[w], 0u, fresh);
-                    rec = old ? old : fresh;
-                }
-                const unsigned long long t = (gen << 40) | seq;
-                bool placed = false;
-                for (int k = 0; k < kSlots && !placed; ++k) {
-                    const size_t slot = static_cast<size_t>(rec - 1) * kSlots + k;
-                    const uint32_t cur = atomicCAS(&s.ext_pore[slot], kNone, pore);
-                    if (cur == kNone || cur == pore) {
-                        atomicMin(&s.ext_time[slot], t);
-                        placed = true;
-                    }
-                }
-                if (!placed) atomicOr(s.err, 2u);
+                continue;
             }
+            owner = __ldcg(gp + wseq / 27);
+        } else {
+            owner = __ldcg(s.claim + w) - 1;
         }
+        if (owner == pore) continue;
+        ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
     }
 }
 
-// Ordered compaction of this generation's same-depth claims: counts per chunk of event slots.
-__global__ void ws_slot_count(const uint32_t* __restrict__ slot_gen, const unsigned int* __restrict__ d_ng,
-                              uint32_t gen, unsigned int* __restrict__ ccount) {
-    const size_t nev = static_cast<size_t>(*d_ng) * 27;
-    const size_t nchunks = (nev + kChunk - 1) / kChunk;
-    __shared__ unsigned int part[32];
-    for (size_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+// Ordered compaction of a generation's same-depth claims (event slots stamped with the
+// generation number), in three steps: counts per chunk of kChunk slots, an exclusive scan of
+// the counts (block 0), and the scatter of the claims in event order.
+__device__ __forceinline__ void ws_slot_count(const uint32_t* slot_gen, unsigned long long nev, uint32_t gen,
+                                              unsigned int* ccount, unsigned int* part) {
+    const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
+    for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
         unsigned int local = 0;
-        for (size_t k = threadIdx.x; k < kChunk; k += blockDim.x) {
-            const size_t e = c * kChunk + k;
-            local += (e < nev && slot_gen[e] == gen) ? 1u : 0u;
+        for (unsigned k = threadIdx.x; k < kChunk; k += blockDim.x) {
+            const unsigned long long e = c * kChunk + k;
+            local += (e < nev && __ldcg(slot_gen + e) == gen) ? 1u : 0u;
         }
         for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
         if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = local;
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned int sum = 0;
-            for (unsigned w = 0; w < (blockDim.x + 31) / 32; ++w) sum += part[w];
+            for (unsigned w = 0; w < blockDim.x / 32; ++w) sum += part[w];
             ccount[c] = sum;
         }
         __syncthreads();
     }
 }
 
-// Exclusive scan of chunk counts (one block); writes the next generation's size.
-__global__ void ws_slot_scan(unsigned int* __restrict__ ccount, const unsigned int* __restrict__ d_ng,
-                             unsigned int* __restrict__ d_ng_next) {
-    const size_t nev = static_cast<size_t>(*d_ng) * 27;
-    const size_t nchunks = (nev + kChunk - 1) / kChunk;
-    __shared__ unsigned int part[1024];
-    const size_t per = (nchunks + blockDim.x - 1) / blockDim.x;
-    unsigned int s = 0;
-    for (size_t k = 0; k < per; ++k) {
-        const size_t c = threadIdx.x * per + k;
-        if (c < nchunks) s += ccount[c];
+__device__ __forceinline__ void ws_slot_scan(unsigned int* ccount, unsigned long long nev, unsigned int* ng_next,
+                                             unsigned int* part) {
+    const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
+    const unsigned long long per = (nchunks + blockDim.x - 1) / blockDim.x;
+    unsigned int sum = 0;
+    for (unsigned long long k = 0; k < per; ++k) {
+        const unsigned long long c = threadIdx.x * per + k;
+        if (c < nchunks) sum += __ldcg(ccount + c);
     }
-    part[threadIdx.x] = s;
+    part[threadIdx.x] = sum;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned int run = 0;
@@ -203,40 +263,37 @@ __global__ void ws_slot_scan(unsigned int* __restrict__ ccount, const unsigned i
             part[t] = run;
             run += v;
         }
-        *d_ng_next = run;
+        *ng_next = run;
     }
     __syncthreads();
     unsigned int run = part[threadIdx.x];
-    for (size_t k = 0; k < per; ++k) {
-        const size_t c = threadIdx.x * per + k;
+    for (unsigned long long k = 0; k < per; ++k) {
+        const unsigned long long c = threadIdx.x * per + k;
         if (c < nchunks) {
-            const unsigned int v = ccount[c];
+            const unsigned int v = __ldcg(ccount + c);
             ccount[c] = run;
             run += v;
         }
     }
 }
 
-// Writes the same-depth claims in event order as the next generation (voxel, pore).
 // blockDim.x == kChunk / 4: each thread owns 4 consecutive slots of the block's chunk.
-__global__ void ws_slot_scatter(const uint32_t* __restrict__ slot_gen, const uint32_t* __restrict__ slot_voxel,
-                                const unsigned int* __restrict__ d_ng, uint32_t gen,
-                                const unsigned int* __restrict__ coff, const uint32_t* __restrict__ gp,
-                                uint32_t* __restrict__ nv, uint32_t* __restrict__ np_) {
-    const size_t nev = static_cast<size_t>(*d_ng) * 27;
-    const size_t nchunks = (nev + kChunk - 1) / kChunk;
-    __shared__ unsigned int warp_sum[32];
-    for (size_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const unsigned int base = coff[c];
-        const size_t e0 = c * kChunk + static_cast<size_t>(threadIdx.x) * 4;
+__device__ __forceinline__ void ws_slot_scatter(const uint32_t* slot_gen, const uint32_t* slot_voxel,
+                                                unsigned long long nev, uint32_t gen, const unsigned int* coff,
+                                                const uint32_t* gp, uint32_t* nv, uint32_t* np_,
+                                                unsigned int* warp_sum) {
+    const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const unsigned int base = __ldcg(coff + c);
+        const unsigned long long e0 = c * kChunk + static_cast<unsigned long long>(threadIdx.x) * 4;
         unsigned int f[4];
         unsigned int mine = 0;
         for (int k = 0; k < 4; ++k) {
-            const size_t e = e0 + k;
-            f[k] = (e < nev && slot_gen[e] == gen) ? 1u : 0u;
+            const unsigned long long e = e0 + k;
+            f[k] = (e < nev && __ldcg(slot_gen + e) == gen) ? 1u : 0u;
             mine += f[k];
         }
-        const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         unsigned int incl = mine;
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
@@ -245,7 +302,7 @@ __global__ void ws_slot_scatter(const uint32_t* __restrict__ slot_gen, const uin
         if (lane == 31) warp_sum[warp] = incl;
         __syncthreads();
         if (warp == 0) {
-            const unsigned nw = (blockDim.x + 31) / 32;
+            const unsigned nw = blockDim.x / 32;
             unsigned int wsum = lane < nw ? warp_sum[lane] : 0u;
             for (int o = 1; o < 32; o <<= 1) {
                 const unsigned int t = __shfl_up_sync(0xFFFFFFFFu, wsum, o);
@@ -257,12 +314,52 @@ __global__ void ws_slot_scatter(const uint32_t* __restrict__ slot_gen, const uin
         unsigned int pos = base + (warp ? warp_sum[warp - 1] : 0u) + incl - mine;
         for (int k = 0; k < 4; ++k) {
             if (!f[k]) continue;
-            const size_t e = e0 + k;
-            nv[pos] = slot_voxel[e];
-            np_[pos] = gp[e / 27];
+            const unsigned long long e = e0 + k;
+            nv[pos] = __ldcg(slot_voxel + e);
+            np_[pos] = __ldcg(gp + e / 27);
             ++pos;
         }
         __syncthreads();
+    }
+}
+
+// Up to max_gens generations of one depth in a single cooperative launch, with grid-wide
+// barriers between the phases. ng[2] holds the two frontier sizes; the frontier starts on
+// side `cur`. out[0] = generations run, out[1] = the side holding the next frontier.
+__global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t* gv0, uint32_t* gp0, uint32_t* gv1,
+                                                             uint32_t* gp1, unsigned int* ng, unsigned int* ccount,
+                                                             uint32_t depth, unsigned long long gen0, int max_gens,
+                                                             int cur, unsigned long long* out) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ unsigned int part[kChunk / 4];
+    const unsigned long long tid = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+    const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    unsigned long long gen = gen0;
+    int it = 0;
+    for (; it < max_gens; ++it) {
+        const unsigned long long nev = static_cast<unsigned long long>(__ldcg(ng + cur)) * 27;
+        if (nev == 0) break;
+        ++gen;
+        const uint32_t* gv = cur ? gv1 : gv0;
+        const uint32_t* gp = cur ? gp1 : gp0;
+        uint32_t* nv = cur ? gv0 : gv1;
+        uint32_t* np_ = cur ? gp0 : gp1;
+        ws_touch<0>(s, gv, gp, nev, depth, gen, tid, stride);
+        grid.sync();
+        ws_touch<1>(s, gv, gp, nev, depth, gen, tid, stride);
+        grid.sync();
+        ws_slot_count(s.slot_gen, nev, static_cast<uint32_t>(gen), ccount, part);
+        grid.sync();
+        if (blockIdx.x == 0) ws_slot_scan(ccount, nev, ng + (cur ^ 1), part);
+        grid.sync();
+        ws_slot_scatter(s.slot_gen, s.slot_voxel, nev, static_cast<uint32_t>(gen), ccount, gp, nv, np_, part);
+        grid.sync();
+        cur ^= 1;
+    }
+    if (tid == 0) {
+        out[0] = static_cast<unsigned long long>(it);
+        out[1] = static_cast<unsigned long long>(cur);
     }
 }
 
@@ -454,118 +551,154 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ws.claim = buf<uint32_t>(ctx, "ws.claim", n);
     ws.ckey = buf<unsigned long long>(ctx, "ws.ckey", n);
     ws.ext = buf<uint32_t>(ctx, "ws.ext", n);
-    ws.ext_cap = static_cast<uint32_t>(std::min<size_t>(std::max<size_t>(n / 8, 4096), 0x7FFFFFFF / kSlots));
-    ws.ext_pore = buf<uint32_t>(ctx, "ws.ext_pore", static_cast<size_t>(ws.ext_cap) * kSlots);
-    ws.ext_time = buf<unsigned long long>(ctx, "ws.ext_time", static_cast<size_t>(ws.ext_cap) * kSlots);
     ws.ext_count = reinterpret_cast<unsigned int*>(d_count + 1);
     ws.err = reinterpret_cast<unsigned int*>(d_count + 2);
     ws.pbound = buf<unsigned int>(ctx, "ws.pbound", npores);
-    PMA_CUDA(cudaMemsetAsync(d_count, 0, 32, s));
-    PMA_CUDA(cudaMemsetAsync(ws.ext_pore, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 4, s));
-    PMA_CUDA(cudaMemsetAsync(ws.ext_time, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 8, s));
-    PMA_CUDA(cudaMemsetAsync(ws.pbound, 0, std::max<size_t>(npores, 1) * 4, s));
-    ws_init<<<G, 256, 0, s>>>(n, ws.claim, ws.ckey, ws.ext);
-    ctx->check_launch("ws_init");
-
-    // Buckets: capacity = voxels of that crad + seeds of that radius.
-    unsigned int* hist = buf<unsigned int>(ctx, "ws.hist", nb);
-    PMA_CUDA(cudaMemsetAsync(hist, 0, nb * 4ull, s));
-    ws_histograms<<<G, 256, 0, s>>>(crad2, n, hist);
-    ctx->check_launch("ws_histograms");
-    std::vector<unsigned int> h_hist(nb);
-    PMA_CUDA(cudaMemcpyAsync(h_hist.data(), hist, nb * 4ull, cudaMemcpyDeviceToHost, s));
-    ctx->sync();
-    std::vector<unsigned long long> boff(nb + 1, 0);
-    size_t max_bucket = 1;
-    for (uint32_t b = 0; b < nb; ++b) {
-        const unsigned long long c = static_cast<unsigned long long>(h_hist[b]) + seed_hist[b];
-        boff[b + 1] = boff[b] + c;
-        max_bucket = std::max<size_t>(max_bucket, c);
-    }
-    const unsigned long long total = boff[nb];
-    auto* d_boff = buf<unsigned long long>(ctx, "ws.boff", nb + 1);
-    ws.boff = d_boff;
-    ws.bfill = buf<unsigned int>(ctx, "ws.bfill", nb);
-    ws.ent_time = buf<unsigned long long>(ctx, "ws.ent_time", total);
-    ws.ent_val = buf<unsigned long long>(ctx, "ws.ent_val", total);
-    auto* srt_time = buf<unsigned long long>(ctx, "ws.srt_time", max_bucket);
-    auto* srt_val = buf<unsigned long long>(ctx, "ws.srt_val", max_bucket);
-    const size_t max_events = max_bucket * 27;
-    ws.slot_gen = buf<uint32_t>(ctx, "ws.slot_gen", max_events);
-    ws.slot_voxel = buf<uint32_t>(ctx, "ws.slot_voxel", max_events);
-    PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));  // generations start at 1
-    unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", (max_events + kChunk - 1) / kChunk);
-    PMA_CUDA(cudaMemcpyAsync(d_boff, boff.data(), (nb + 1) * 8ull, cudaMemcpyHostToDevice, s));
-    std::vector<unsigned int> h_fill(nb, 0);
-    if (npores) {
-        std::vector<unsigned long long> a(3 * npores);
-        for (size_t k = 0; k < npores; ++k) {
-            const uint32_t b = pores[k].seed_r2;
-            a[k] = boff[b] + h_fill[b]++;
-            a[npores + k] = k;  // seeds come first in their bucket, in pore-id order
-            a[2 * npores + k] = (static_cast<unsigned long long>(k) << 32) | seed_voxel[k];
-        }
-        auto* d_a = buf<unsigned long long>(ctx, "ws.seed_at", 3 * npores);
-        PMA_CUDA(cudaMemcpyAsync(d_a, a.data(), 3 * npores * 8, cudaMemcpyHostToDevice, s));
-        ws_seed_entries<<<grid_for(ctx, npores), 256, 0, s>>>(d_a, npores, ws.ent_time, ws.ent_val);
-        ctx->check_launch("ws_seed_entries");
-        uint32_t* d_seed = buf<uint32_t>(ctx, "ws.seedvox", npores);
-        PMA_CUDA(cudaMemcpyAsync(d_seed, seed_voxel.data(), npores * 4, cudaMemcpyHostToDevice, s));
-        ws_seed<<<grid_for(ctx, npores), 256, 0, s>>>(d_seed, npores, ws.claim);
-        ctx->check_launch("ws_seed");
-        ctx->sync();
-    }
-    PMA_CUDA(cudaMemcpyAsync(ws.bfill, h_fill.data(), nb * 4ull, cudaMemcpyHostToDevice, s));
-    ctx->sync();
-
-    // Depth sweep (WatershedComputer.cpp:80-102).
-    uint32_t* gvb[2] = {buf<uint32_t>(ctx, "ws.gv0", max_bucket), buf<uint32_t>(ctx, "ws.gv1", max_bucket)};
-    uint32_t* gpb[2] = {buf<uint32_t>(ctx, "ws.gp0", max_bucket), buf<uint32_t>(ctx, "ws.gp1", max_bucket)};
-    const unsigned tgrid = static_cast<unsigned>(ctx->num_sms * 8);
-    unsigned long long gen = 0;
-    unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
-    for (int64_t depth = static_cast<int64_t>(nb) - 1; depth >= 0; --depth) {
-        if (boff[depth + 1] == boff[depth]) continue;
-        PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + depth, 4, cudaMemcpyDeviceToHost, s));
-        ctx->sync();
-        const size_t n0 = h_small[0];
-        if (n0 == 0) continue;
-        sort_pairs(ctx, ws.ent_time + boff[depth], srt_time, ws.ent_val + boff[depth], srt_val,
-                   static_cast<int64_t>(n0));
-        int cur = 0;
-        ws_unpack_entries<<<grid_for(ctx, n0), 256, 0, s>>>(srt_val, n0, gvb[cur], gpb[cur]);
-        ctx->check_launch("ws_unpack_entries");
-        h_small[2] = static_cast<unsigned int>(n0);
-        PMA_CUDA(cudaMemcpyAsync(d_ng + cur, &h_small[2], 4, cudaMemcpyHostToDevice, s));
-        KernelTimer kt(ctx, "ws_generations");
-        while (true) {
-            for (int k = 0; k < kGensPerSync; ++k) {
-                ++gen;
-                const int nxt = cur ^ 1;
-                const uint32_t dep = static_cast<uint32_t>(depth);
-                const uint32_t g32 = static_cast<uint32_t>(gen);
-                ws_touch<0><<<tgrid, 128, 0, s>>>(ws, gvb[cur], gpb[cur], d_ng + cur, dep, gen);
-                ws_touch<1><<<tgrid, 128, 0, s>>>(ws, gvb[cur], gpb[cur], d_ng + cur, dep, gen);
-                ws_touch<2><<<tgrid, 128, 0, s>>>(ws, gvb[cur], gpb[cur], d_ng + cur, dep, gen);
-                ws_slot_count<<<tgrid, 256, 0, s>>>(ws.slot_gen, d_ng + cur, g32, ccount);
-                ws_slot_scan<<<1, 1024, 0, s>>>(ccount, d_ng + cur, d_ng + nxt);
-                ws_slot_scatter<<<tgrid, kChunk / 4, 0, s>>>(ws.slot_gen, ws.slot_voxel, d_ng + cur, g32,
-                                                              ccount, gpb[cur], gvb[nxt], gpb[nxt]);
-                ctx->count_launch(6);
-                cur = nxt;
-            }
-            PMA_CUDA(cudaGetLastError());
-            PMA_CUDA(cudaMemcpyAsync(h_small + 1, d_ng + cur, 4, cudaMemcpyDeviceToHost, s));
-            ctx->sync();
-            if (h_small[1] == 0) break;
-            PMA_REQUIRE(gen < (1ull << 23), PMA_ERR_LIMIT, "pma_watershed: generation limit reached");
-        }
-    }
+    // Shared-voxel records: a first guess of n/32; the pool doubles (copying the records)
+    // whenever it is more than half used at a host synchronisation point, and a flood that
+    // still runs out is redone with four times as many (up to one per voxel).
+    const size_t max_records = std::min<size_t>(n + 4096, 0x7FFFFFFF / kSlots);
+    size_t ext_cap = std::min<size_t>(std::max<size_t>(n / 32, 4096), max_records);
+    int ext_side = 0;  // which of two scratch tags holds the records
+    auto ext_tag = [&](const char* base) { return std::string(base) + (ext_side ? ".1" : ".0"); };
+    auto grow_records = [&](size_t used) {
+        if (2 * used <= ws.ext_cap || ws.ext_cap >= max_records) return;
+        const size_t old_cap = ws.ext_cap;
+        const size_t cap2 = std::min<size_t>(std::max<size_t>(2 * old_cap, 4 * used), max_records);
+        const std::string old_p = ext_tag("ws.ext_pore"), old_t = ext_tag("ws.ext_time");
+        ext_side ^= 1;
+        auto* np_ = buf<uint32_t>(ctx, ext_tag("ws.ext_pore").c_str(), cap2 * kSlots);
+        auto* nt_ = buf<unsigned long long>(ctx, ext_tag("ws.ext_time").c_str(), cap2 * kSlots);
+        PMA_CUDA(cudaMemcpyAsync(np_, ws.ext_pore, old_cap * kSlots * 4, cudaMemcpyDeviceToDevice, s));
+        PMA_CUDA(cudaMemcpyAsync(nt_, ws.ext_time, old_cap * kSlots * 8, cudaMemcpyDeviceToDevice, s));
+        PMA_CUDA(cudaMemsetAsync(np_ + old_cap * kSlots, 0xFF, (cap2 - old_cap) * kSlots * 4, s));
+        PMA_CUDA(cudaMemsetAsync(nt_ + old_cap * kSlots, 0xFF, (cap2 - old_cap) * kSlots * 8, s));
+        ctx->release(old_p);
+        ctx->release(old_t);
+        ws.ext_pore = np_;
+        ws.ext_time = nt_;
+        ws.ext_cap = static_cast<uint32_t>(cap2);
+    };
     unsigned int h_err = 0;
-    PMA_CUDA(cudaMemcpyAsync(&h_err, ws.err, 4, cudaMemcpyDeviceToHost, s));
-    ctx->sync();
-    PMA_REQUIRE(!(h_err & 1u), PMA_ERR_MEMORY, "pma_watershed: shared-voxel records exhausted");
+    for (;;) {
+        const size_t start_cap = ext_cap;
+        ws.ext_cap = static_cast<uint32_t>(ext_cap);
+        ws.ext_pore = buf<uint32_t>(ctx, ext_tag("ws.ext_pore").c_str(), static_cast<size_t>(ws.ext_cap) * kSlots);
+        ws.ext_time = buf<unsigned long long>(ctx, ext_tag("ws.ext_time").c_str(),
+                                              static_cast<size_t>(ws.ext_cap) * kSlots);
+        PMA_CUDA(cudaMemsetAsync(d_count, 0, 32, s));
+        PMA_CUDA(cudaMemsetAsync(ws.ext_pore, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 4, s));
+        PMA_CUDA(cudaMemsetAsync(ws.ext_time, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 8, s));
+        PMA_CUDA(cudaMemsetAsync(ws.pbound, 0, std::max<size_t>(npores, 1) * 4, s));
+        ws_init<<<G, 256, 0, s>>>(n, ws.claim, ws.ckey, ws.ext);
+        ctx->check_launch("ws_init");
+
+        // Buckets: capacity = voxels of that crad + seeds of that radius.
+        unsigned int* hist = buf<unsigned int>(ctx, "ws.hist", nb);
+        PMA_CUDA(cudaMemsetAsync(hist, 0, nb * 4ull, s));
+        ws_histograms<<<G, 256, 0, s>>>(crad2, n, nb, hist);
+        ctx->check_launch("ws_histograms");
+        std::vector<unsigned int> h_hist(nb);
+        PMA_CUDA(cudaMemcpyAsync(h_hist.data(), hist, nb * 4ull, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        std::vector<unsigned long long> boff(nb + 1, 0);
+        size_t max_bucket = 1;
+        for (uint32_t b = 0; b < nb; ++b) {
+            const unsigned long long c = static_cast<unsigned long long>(h_hist[b]) + seed_hist[b];
+            boff[b + 1] = boff[b] + c;
+            max_bucket = std::max<size_t>(max_bucket, c);
+        }
+        const unsigned long long total = boff[nb];
+        auto* d_boff = buf<unsigned long long>(ctx, "ws.boff", nb + 1);
+        ws.boff = d_boff;
+        ws.bfill = buf<unsigned int>(ctx, "ws.bfill", nb);
+        ws.ent_time = buf<unsigned long long>(ctx, "ws.ent_time", total);
+        ws.ent_val = buf<unsigned long long>(ctx, "ws.ent_val", total);
+        auto* srt_time = buf<unsigned long long>(ctx, "ws.srt_time", max_bucket);
+        auto* srt_val = buf<unsigned long long>(ctx, "ws.srt_val", max_bucket);
+        const size_t max_events = max_bucket * 27;
+        ws.slot_gen = buf<uint32_t>(ctx, "ws.slot_gen", max_events);
+        ws.slot_voxel = buf<uint32_t>(ctx, "ws.slot_voxel", max_events);
+        PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));  // generations start at 1
+        unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", (max_events + kChunk - 1) / kChunk);
+        PMA_CUDA(cudaMemcpyAsync(d_boff, boff.data(), (nb + 1) * 8ull, cudaMemcpyHostToDevice, s));
+        std::vector<unsigned int> h_fill(nb, 0);
+        if (npores) {
+            std::vector<unsigned long long> a(3 * npores);
+            for (size_t k = 0; k < npores; ++k) {
+                const uint32_t b = pores[k].seed_r2;
+                a[k] = boff[b] + h_fill[b]++;
+                a[npores + k] = k;  // seeds come first in their bucket, in pore-id order
+                a[2 * npores + k] = (static_cast<unsigned long long>(k) << 32) | seed_voxel[k];
+            }
+            auto* d_a = buf<unsigned long long>(ctx, "ws.seed_at", 3 * npores);
+            PMA_CUDA(cudaMemcpyAsync(d_a, a.data(), 3 * npores * 8, cudaMemcpyHostToDevice, s));
+            ws_seed_entries<<<grid_for(ctx, npores), 256, 0, s>>>(d_a, npores, ws.ent_time, ws.ent_val);
+            ctx->check_launch("ws_seed_entries");
+            uint32_t* d_seed = buf<uint32_t>(ctx, "ws.seedvox", npores);
+            PMA_CUDA(cudaMemcpyAsync(d_seed, seed_voxel.data(), npores * 4, cudaMemcpyHostToDevice, s));
+            ws_seed<<<grid_for(ctx, npores), 256, 0, s>>>(d_seed, npores, ws.claim);
+            ctx->check_launch("ws_seed");
+            ctx->sync();
+        }
+        PMA_CUDA(cudaMemcpyAsync(ws.bfill, h_fill.data(), nb * 4ull, cudaMemcpyHostToDevice, s));
+        ctx->sync();
+
+        // Depth sweep (WatershedComputer.cpp:80-102).
+        uint32_t* gvb[2] = {buf<uint32_t>(ctx, "ws.gv0", max_bucket), buf<uint32_t>(ctx, "ws.gv1", max_bucket)};
+        uint32_t* gpb[2] = {buf<uint32_t>(ctx, "ws.gp0", max_bucket), buf<uint32_t>(ctx, "ws.gp1", max_bucket)};
+        // cooperative grid: every block resident at once (grid-wide barriers)
+        int per_sm = 0;
+        PMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_generations, kChunk / 4, 0));
+        PMA_REQUIRE(per_sm > 0, PMA_ERR_CUDA, "pma_watershed: generation kernel does not fit an SM");
+        const unsigned coop_grid = static_cast<unsigned>(ctx->num_sms * std::min(per_sm, 8));
+        unsigned long long gen = 0;
+        unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
+        auto* d_out = buf<unsigned long long>(ctx, "ws.coop_out", 2);
+        unsigned long long* h_out = reinterpret_cast<unsigned long long*>(h_small + 8);
+        for (int64_t depth = static_cast<int64_t>(nb) - 1; depth >= 0; --depth) {
+            if (boff[depth + 1] == boff[depth]) continue;
+            PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + depth, 4, cudaMemcpyDeviceToHost, s));
+            PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            grow_records(h_small[4]);
+            const size_t n0 = h_small[0];
+            if (n0 == 0) continue;
+            sort_pairs(ctx, ws.ent_time + boff[depth], srt_time, ws.ent_val + boff[depth], srt_val,
+                       static_cast<int64_t>(n0));
+            int cur = 0;
+            ws_unpack_entries<<<grid_for(ctx, n0), 256, 0, s>>>(srt_val, n0, gvb[cur], gpb[cur]);
+            ctx->check_launch("ws_unpack_entries");
+            h_small[2] = static_cast<unsigned int>(n0);
+            PMA_CUDA(cudaMemcpyAsync(d_ng + cur, &h_small[2], 4, cudaMemcpyHostToDevice, s));
+            KernelTimer kt(ctx, "ws_generations");
+            while (true) {
+                const uint32_t dep = static_cast<uint32_t>(depth);
+                int gens = kGensPerLaunch;
+                void* args[] = {&ws, &gvb[0], &gpb[0], &gvb[1], &gpb[1], &d_ng, &ccount,
+                                const_cast<uint32_t*>(&dep), &gen, &gens, &cur, &d_out};
+                PMA_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ws_generations), coop_grid,
+                                                     kChunk / 4, args, 0, s));
+                ctx->count_launch(1);
+                PMA_CUDA(cudaMemcpyAsync(h_out, d_out, 16, cudaMemcpyDeviceToHost, s));
+                PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
+                PMA_CUDA(cudaMemcpyAsync(h_small + 6, d_ng, 8, cudaMemcpyDeviceToHost, s));
+                ctx->sync();
+                gen += h_out[0];
+                cur = static_cast<int>(h_out[1]);
+                grow_records(h_small[4]);
+                if (h_small[6 + cur] == 0) break;
+                PMA_REQUIRE(gen + kGensPerLaunch < kMaxGen, PMA_ERR_LIMIT, "pma_watershed: generation limit reached");
+            }
+        }
+        PMA_CUDA(cudaMemcpyAsync(&h_err, ws.err, 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        if (!(h_err & 1u)) break;
+        PMA_REQUIRE(start_cap < max_records, PMA_ERR_MEMORY, "pma_watershed: shared-voxel records exhausted");
+        ext_cap = std::min<size_t>(std::max<size_t>(ws.ext_cap, start_cap * 4), max_records);
+    }
     PMA_REQUIRE(!(h_err & 2u), PMA_ERR_LIMIT, "pma_watershed: more than 7 pores touch one voxel");
+    PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
 
     // Volumes, labels and shared voxels.
     auto* pvol = buf<unsigned long long>(ctx, "ws.pvol", npores);

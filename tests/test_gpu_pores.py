@@ -111,3 +111,18 @@ def test_watershed_accepts_pores_read_back(ctx, ref_cases):
     ws, ws_table = pma.assign_watershed_ids(ctx, table, crad2, mx)
     assert digest(ws.cpu().numpy().view(np.uint32)) == rec["digests"]["PoreThroatIdsWatershed"]
     assert ws_table.rows() == (rows(rec["pores_ws"]), rows(rec["throats_ws"]))
+
+
+def test_watershed_with_most_voxels_shared(ctx, oracle_mod):
+    """Uncorrelated noise (porosity 0.7): nearly every void voxel touches several pores, far
+    more shared voxels than the watershed's first guess of records, so the flood is redone
+    with more records; the result must still equal the oracle's."""
+    rng = np.random.default_rng(12)
+    vol = (rng.random((40, 44, 36)) > 0.7).astype(np.uint8)
+    g = _gpu_pipeline(ctx, vol, False)
+    r = oracle_mod.full(vol, geodesic_too=False)["pores"]
+    assert g["table"][0] == r.pores
+    assert (g["ws"] == r.labels_ws).all()
+    pws, tws = g["ws_table"]
+    assert pws == r.pores_ws and tws == r.throats_ws
+    assert len(tws) > 0
