@@ -54,9 +54,10 @@ int pma_abi_version(void);
 typedef struct pma_ctx pma_ctx;
 int pma_ctx_create(int device, pma_ctx** out);
 int pma_ctx_destroy(pma_ctx* ctx);
-/* Runs subsequent work of ctx on an existing cudaStream_t (NULL = the context's own). */
+/* Runs subsequent work of ctx on an existing cudaStream_t (NULL = a new stream of the
+ * context's own; pass cudaStreamLegacy to share the legacy default stream). */
 int pma_ctx_set_stream(pma_ctx* ctx, void* cuda_stream);
-/* Number of this library's kernels launched through ctx since creation. */
+/* Number of this library's kernels launched through ctx (and its batch lanes) since creation. */
 uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
 /* Opt-in kernel timing: with timing on, the hot kernels are bracketed by CUDA events on
  * the context's stream. The report is a JSON object {"kernel": [total_ms, launches], ...}
@@ -217,6 +218,68 @@ typedef struct pma_options {
 
 int pma_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims,
                       const pma_options* opts, pma_outputs* out);
+
+/* ---------------------------------------------------------------------------------
+ * Batched form: many independent volumes of uneven sizes in one call. No counterpart in
+ * the reference, which processes sample folders one after another
+ * (CommandLineDispatcher.cpp:62-71).
+ * ------------------------------------------------------------------------------- */
+typedef struct pma_batch_item {
+    const uint8_t* solid;       /* [z][x][y] volume, non-zero = solid: host memory, or
+                                   device memory when the call is resident */
+    pma_dims dims;
+    int status;                 /* set by the call: this volume's pma_status */
+    pma_outputs* out;           /* as for pma_pipeline_host; with resident = 1 its field
+                                   pointers are device pointers (NULL = not kept) */
+} pma_batch_item;
+
+/* Runs the whole chain (options as pma_pipeline_host) on n volumes with up to `lanes` of them
+ * in flight at once (0 = 8, at most 64), each lane with its own stream, host thread and
+ * scratch memory, kept by ctx for later calls. Every volume's results equal a separate
+ * pma_pipeline_host call. Returns PMA_OK when all volumes succeeded, else the status of the
+ * first failing one (pma_last_error names it); the other volumes still complete. */
+int pma_pipeline_batch(pma_ctx* ctx, pma_batch_item* items, size_t n, const pma_options* opts,
+                       int resident, int lanes);
+
+/* ---------------------------------------------------------------------------------
+ * Serving: a request loop with continuous batching under a device-memory budget. No
+ * counterpart in the reference. Requests are admitted in arrival order as lanes (child
+ * contexts with their own stream, scratch and host thread) and budget free up; requests in
+ * flight overlap on the device, and each request's fields stay on the device from the first
+ * stage to the last. Every result equals a separate pma_pipeline_host call.
+ * ------------------------------------------------------------------------------- */
+typedef struct pma_server pma_server;
+
+typedef struct pma_server_config {
+    int lanes;                  /* requests in flight at most (0 = 8, at most 64) */
+    int pad_;
+    uint64_t memory_budget;     /* device bytes for all lanes' fields and scratch (0 = 120 GiB) */
+    pma_options options;        /* as for pma_pipeline_host */
+} pma_server_config;
+
+typedef struct pma_server_stats {
+    uint64_t submitted, completed, failed, rejected;
+    uint64_t queued;
+    uint64_t peak_reserved_bytes;   /* largest sum of lane reservations at an admission */
+    uint64_t resident_bytes;        /* lanes' device scratch now */
+    double bytes_per_voxel;         /* footprint estimate used for admission */
+    uint32_t max_in_flight;
+    uint32_t pad_;
+} pma_server_stats;
+
+int pma_server_create(pma_ctx* ctx, const pma_server_config* cfg, pma_server** out);
+/* Queues one volume (host memory, [z][x][y], non-zero = solid); h_solid and out (host output
+ * buffers and tables as for pma_pipeline_host) must stay valid until the request completes. */
+int pma_server_submit(pma_server* srv, const uint8_t* h_solid, pma_dims dims, pma_outputs* out,
+                      uint64_t* ticket);
+/* Waits for a request (timeout_ms < 0: no limit; PMA_ERR_LIMIT when it runs out) and
+ * returns PMA_OK with *status = the request's own status (PMA_ERR_MEMORY if it alone exceeds
+ * the budget) and its latency from submission to completion. A ticket is waited for once. */
+int pma_server_wait(pma_server* srv, uint64_t ticket, int64_t timeout_ms, int* status,
+                    double* latency_ms);
+int pma_server_get_stats(pma_server* srv, pma_server_stats* out);
+/* Completes the queued requests, then releases the lanes. */
+int pma_server_destroy(pma_server* srv);
 
 /* ---------------------------------------------------------------------------------
  * Folder-level drop-in for the command-line modes (CommandLineDispatcher.cpp:34-72,

@@ -21,7 +21,8 @@ from .capi import D3Q7, D3Q27, MODE_ALL, MODE_APT, MODE_EDT, MODE_RIB, MODE_SPD,
 
 __all__ = ["Context", "Table", "compute_euclidean_distances", "set_containing_balls",
            "assign_pore_and_throat_ids", "remove_empty_pores", "assign_watershed_ids",
-           "compute_shortest_path_distances", "run_folder", "pipeline_host", "D3Q7", "D3Q27",
+           "compute_shortest_path_distances", "run_folder", "pipeline_host", "pipeline_batch",
+           "Server", "D3Q7", "D3Q27",
            "MODE_ALL", "MODE_EDT", "MODE_RIB", "MODE_APT", "MODE_SPD", "PmaError"]
 
 
@@ -37,7 +38,10 @@ class Context:
         if stream is None:
             stream = torch.cuda.current_stream(device)
         self.stream = stream
-        capi.check(capi.lib().pma_ctx_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+        handle = stream.cuda_stream
+        if handle == 0:  # torch's default stream is CUDA's legacy default stream
+            handle = capi.CUDA_STREAM_LEGACY
+        capi.check(capi.lib().pma_ctx_set_stream(h, ctypes.c_void_p(handle)))
 
     def close(self):
         if self.handle:
@@ -99,6 +103,10 @@ class Table:
 
     def rows(self):
         return capi.table_to_python(self.handle)
+
+    def counts(self):
+        """(number of pores, number of shared types) without converting the rows."""
+        return (capi.lib().pma_table_npores(self.handle), capi.lib().pma_table_nthroats(self.handle))
 
     def __del__(self):
         if getattr(self, "handle", None):
@@ -190,6 +198,42 @@ def run_folder(ctx, base_folder, mode=MODE_ALL):
     capi.check(capi.lib().pma_run_folder(ctx.handle, str(base_folder).encode(), mode))
 
 
+_KINDS = {"edt2": "uint32", "crad2": "uint32", "cx": "uint32", "cy": "uint32", "cz": "uint32",
+          "maxball_mask": "uint8", "pore_labels": "uint32", "watershed_labels": "uint32",
+          "dist_f32": "float32", "dist_f64": "float64", "cavity": "uint32"}
+
+
+def _bind_outputs(out, shape, fields, given, device=None):
+    """Points the Outputs fields at numpy arrays (device None) or torch CUDA tensors."""
+    import numpy as np
+    res = dict(given or {})
+    for name in fields:
+        arr = res.get(name)
+        if arr is None:
+            if device is None:
+                arr = np.empty(shape, dtype=_KINDS[name])
+            else:
+                import torch
+                dt = {"uint32": torch.int32, "uint8": torch.uint8, "float32": torch.float32,
+                      "float64": torch.float64}[_KINDS[name]]
+                arr = torch.empty(shape, dtype=dt, device=device)
+            res[name] = arr
+        addr = arr.ctypes.data if device is None else arr.data_ptr()
+        setattr(out, name, ctypes.cast(addr, type(getattr(out, name))))
+    return res
+
+
+def _collect(out, res):
+    res["max_edt2"] = out.edt_stats.max_edt2
+    res["maximum_balls_count"] = out.maximum_balls_count
+    res["pores"] = Table(out.pores) if out.pores else None
+    res["watershed"] = Table(out.watershed) if out.watershed else None
+    res["cavities"] = [(c.id, c.seed_x, c.seed_y, c.seed_z, c.distance_to_center, c.void_count,
+                        c.reached_walls, c.reaches_all_walls)
+                       for c in out.cavities[:out.n_cavities]]
+    return res
+
+
 def pipeline_host(ctx, solid_np, stencil=D3Q27, run_pores=True, run_geodesic=True, fp64=False,
                   fields=("watershed_labels", "dist_f32"), out_arrays=None):
     """Whole pipeline on a host (SZ, SX, SY) uint8 array through pma_pipeline_host (the
@@ -199,27 +243,100 @@ def pipeline_host(ctx, solid_np, stencil=D3Q27, run_pores=True, run_geodesic=Tru
     import numpy as np
     solid_np = np.ascontiguousarray(solid_np, dtype=np.uint8)
     out = capi.Outputs()
-    res = dict(out_arrays or {})
-    kinds = {"edt2": np.uint32, "crad2": np.uint32, "cx": np.uint32, "cy": np.uint32,
-             "cz": np.uint32, "maxball_mask": np.uint8, "pore_labels": np.uint32,
-             "watershed_labels": np.uint32, "dist_f32": np.float32, "dist_f64": np.float64,
-             "cavity": np.uint32}
-    for name in fields:
-        arr = res.get(name)
-        if arr is None:
-            arr = np.empty(solid_np.shape, dtype=kinds[name])
-            res[name] = arr
-        ctype = type(getattr(out, name))
-        setattr(out, name, ctypes.cast(arr.ctypes.data, ctype))
+    res = _bind_outputs(out, solid_np.shape, fields, out_arrays)
     opts = capi.Options(stencil, int(run_pores), int(run_geodesic), int(fp64))
     capi.check(capi.lib().pma_pipeline_host(ctx.handle, solid_np.ctypes.data, capi.Dims(
         solid_np.shape[1], solid_np.shape[2], solid_np.shape[0]), ctypes.byref(opts),
         ctypes.byref(out)))
-    res["max_edt2"] = out.edt_stats.max_edt2
-    res["maximum_balls_count"] = out.maximum_balls_count
-    res["pores"] = Table(out.pores) if out.pores else None
-    res["watershed"] = Table(out.watershed) if out.watershed else None
-    res["cavities"] = [(c.id, c.seed_x, c.seed_y, c.seed_z, c.distance_to_center, c.void_count,
-                        c.reached_walls, c.reaches_all_walls)
-                       for c in out.cavities[:out.n_cavities]]
+    return _collect(out, res)
+
+
+def pipeline_batch(ctx, volumes, stencil=D3Q27, run_pores=True, run_geodesic=True, fp64=False,
+                   fields=("watershed_labels", "dist_f32"), resident=False, lanes=0, out_arrays=None):
+    """Whole pipeline on many independent (SZ, SX, SY) volumes through pma_pipeline_batch.
+    Host numpy volumes give numpy outputs; with resident=True the volumes are uint8 CUDA
+    tensors and the outputs CUDA tensors (uint32 fields in int32 tensors). Returns one dict
+    per volume, as pipeline_host does. out_arrays may supply one dict of outputs per volume."""
+    import numpy as np
+    n = len(volumes)
+    items = (capi.BatchItem * max(n, 1))()
+    outs = [capi.Outputs() for _ in range(n)]
+    results, keep = [], []
+    for i, v in enumerate(volumes):
+        if resident:
+            assert v.is_cuda and v.is_contiguous() and v.dtype.itemsize == 1
+            addr, shape, dev = v.data_ptr(), tuple(v.shape), v.device
+        else:
+            v = np.ascontiguousarray(v, dtype=np.uint8)
+            addr, shape, dev = v.ctypes.data, v.shape, None
+        keep.append(v)
+        given = out_arrays[i] if out_arrays else None
+        results.append(_bind_outputs(outs[i], shape, fields, given, dev))
+        items[i].solid = addr
+        items[i].dims = capi.Dims(shape[1], shape[2], shape[0])
+        items[i].out = ctypes.pointer(outs[i])
+    opts = capi.Options(stencil, int(run_pores), int(run_geodesic), int(fp64))
+    status = capi.lib().pma_pipeline_batch(ctx.handle, items, n, ctypes.byref(opts), int(resident),
+                                           int(lanes))
+    res = [_collect(outs[i], results[i]) for i in range(n)]
+    capi.check(status)
     return res
+
+
+class Server:
+    """Request loop with continuous batching (pma_server_*): volumes are admitted in arrival
+    order as lanes and device memory free up, and run concurrently on the device."""
+
+    def __init__(self, ctx, lanes=8, memory_budget=0, stencil=D3Q27, run_pores=True,
+                 run_geodesic=True, fp64=False):
+        cfg = capi.ServerConfig(lanes, 0, memory_budget,
+                                capi.Options(stencil, int(run_pores), int(run_geodesic), int(fp64)))
+        h = ctypes.c_void_p()
+        capi.check(capi.lib().pma_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h
+        self._pending = {}
+
+    def submit(self, solid_np, fields=("watershed_labels", "dist_f32"), out_arrays=None):
+        """Queues a host (SZ, SX, SY) volume; returns its ticket."""
+        import numpy as np
+        solid_np = np.ascontiguousarray(solid_np, dtype=np.uint8)
+        out = capi.Outputs()
+        res = _bind_outputs(out, solid_np.shape, fields, out_arrays)
+        t = ctypes.c_uint64()
+        capi.check(capi.lib().pma_server_submit(self.handle, solid_np.ctypes.data, capi.Dims(
+            solid_np.shape[1], solid_np.shape[2], solid_np.shape[0]), ctypes.byref(out), ctypes.byref(t)))
+        self._pending[t.value] = (solid_np, out, res)
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        """(result dict as pipeline_host returns, latency in ms); raises PmaError on failure."""
+        status = ctypes.c_int()
+        lat = ctypes.c_double()
+        capi.check(capi.lib().pma_server_wait(self.handle, ticket, timeout_ms, ctypes.byref(status),
+                                              ctypes.byref(lat)))
+        _, out, res = self._pending.pop(ticket)
+        res = _collect(out, res)
+        capi.check(status.value)
+        return res, lat.value
+
+    def stats(self):
+        st = capi.ServerStats()
+        capi.check(capi.lib().pma_server_get_stats(self.handle, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in capi.ServerStats._fields_ if name != "pad_"}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            capi.check(capi.lib().pma_server_destroy(self.handle))
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

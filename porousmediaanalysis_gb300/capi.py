@@ -19,6 +19,7 @@ PMA_OK = 0
 STATUS = {0: "PMA_OK", 1: "PMA_ERR_ARGUMENT", 2: "PMA_ERR_CUDA", 3: "PMA_ERR_IO",
           4: "PMA_ERR_MEMORY", 5: "PMA_ERR_LIMIT", 6: "PMA_ERR_INTERNAL"}
 D3Q27, D3Q7 = 0, 1
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream as a stream handle
 MODE_ALL, MODE_EDT, MODE_RIB, MODE_APT, MODE_SPD = 1, 2, 3, 4, 5
 
 
@@ -64,6 +65,24 @@ class Options(ctypes.Structure):
                 ("run_geodesic", ctypes.c_int), ("geodesic_fp64", ctypes.c_int)]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("solid", ctypes.c_void_p), ("dims", Dims), ("status", ctypes.c_int),
+                ("out", ctypes.POINTER(Outputs))]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("pad_", ctypes.c_int), ("memory_budget", ctypes.c_uint64),
+                ("options", Options)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("rejected", ctypes.c_uint64), ("queued", ctypes.c_uint64),
+                ("peak_reserved_bytes", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64),
+                ("bytes_per_voxel", ctypes.c_double), ("max_in_flight", ctypes.c_uint32),
+                ("pad_", ctypes.c_uint32)]
+
+
 _SIGNATURES = {
     "pma_last_error": (ctypes.c_size_t, [ctypes.c_char_p, ctypes.c_size_t]),
     "pma_abi_version": (ctypes.c_int, []),
@@ -77,6 +96,16 @@ _SIGNATURES = {
     "pma_ctx_trim": (ctypes.c_int, [ctypes.c_void_p]),
     "pma_edt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_void_p,
                                ctypes.POINTER(EdtStats), ctypes.c_void_p, ctypes.c_size_t]),
+    "pma_pipeline_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_size_t,
+                                          ctypes.POINTER(Options), ctypes.c_int, ctypes.c_int]),
+    "pma_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerConfig),
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "pma_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.POINTER(Outputs),
+                                         ctypes.POINTER(ctypes.c_uint64)]),
+    "pma_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64,
+                                       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    "pma_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    "pma_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pma_edt_noalloc": (ctypes.c_int, [ctypes.c_void_p, Dims, ctypes.c_void_p, ctypes.POINTER(EdtStats),
                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "pma_containing_balls": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_uint32,

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "pma_internal.h"
@@ -59,51 +60,103 @@ void d2h(pma_ctx* ctx, T* host, const T* dev, size_t n) {
 }  // namespace
 }  // namespace pma
 
+namespace pma {
+
+// The chain on device fields of one volume (f.solid filled); tables and statistics go to out.
+static void run_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const pma_options& o, pma_outputs* out) {
+    const bool geo64 = o.run_geodesic && o.geodesic_fp64;
+    out->pores = nullptr;
+    out->watershed = nullptr;
+    out->n_cavities = 0;
+    if (o.run_pores) {
+        edt(ctx, f.solid, dims, f.edt2, &out->edt_stats, nullptr, 0);
+        containing_balls(ctx, f.edt2, dims, out->edt_stats.max_edt2, f.crad2, f.cx, f.cy, f.cz, f.mask,
+                         &out->maximum_balls_count);
+        out->pores = pores(ctx, f.mask, f.edt2, f.crad2, dims, o.stencil, f.labels);
+        remove_empty_pores(ctx, out->pores, f.labels, dims);
+        out->watershed = watershed(ctx, out->pores, f.crad2, dims, o.stencil, out->edt_stats.max_edt2,
+                                   f.labels_ws);
+    }
+    if (o.run_geodesic && !geo64)
+        out->n_cavities = geodesic<float>(ctx, f.solid, dims, o.stencil, f.dist32, f.cavity, out->cavities, 16);
+    else if (o.run_geodesic)
+        out->n_cavities = geodesic<double>(ctx, f.solid, dims, o.stencil, f.dist64, f.cavity, out->cavities, 16);
+}
+
+static pma_options options_or_default(const pma_options* opts) {
+    pma_options o{PMA_D3Q27, 1, 1, 0};
+    if (opts) o = *opts;
+    return o;
+}
+
+void run_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims, const pma_options& o,
+                       pma_outputs* out) {
+    PMA_REQUIRE(h_solid && out, PMA_ERR_ARGUMENT, "pma_pipeline_host: null argument");
+    check_dims(dims);
+    const size_t n = voxels(dims);
+    const bool geo64 = o.run_geodesic && o.geodesic_fp64;
+    Fields f = alloc_fields(ctx, n, o.run_pores != 0, o.run_geodesic != 0 && !geo64, geo64);
+    if (geo64) f.cavity = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
+    PMA_CUDA(cudaMemcpyAsync(f.solid, h_solid, n, cudaMemcpyHostToDevice, ctx->stream));
+    run_chain(ctx, f, dims, o, out);
+    if (o.run_pores) {
+        d2h(ctx, out->edt2, f.edt2, n);
+        d2h(ctx, out->crad2, f.crad2, n);
+        d2h(ctx, out->cx, f.cx, n);
+        d2h(ctx, out->cy, f.cy, n);
+        d2h(ctx, out->cz, f.cz, n);
+        d2h(ctx, out->maxball_mask, f.mask, n);
+        d2h(ctx, out->pore_labels, f.labels, n);
+        d2h(ctx, out->watershed_labels, f.labels_ws, n);
+    }
+    if (o.run_geodesic) {
+        d2h(ctx, out->dist_f32, f.dist32, n);
+        d2h(ctx, out->dist_f64, f.dist64, n);
+        d2h(ctx, out->cavity, f.cavity, n);
+    }
+    ctx->sync();
+}
+
+void run_pipeline_device(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, const pma_options& o,
+                         pma_outputs* out) {
+    PMA_REQUIRE(d_solid && out, PMA_ERR_ARGUMENT, "pma_pipeline_batch: null argument");
+    check_dims(dims);
+    const size_t n = voxels(dims);
+    const bool geo64 = o.run_geodesic && o.geodesic_fp64;
+    // caller's device buffers where given, scratch of the context for the rest
+    Fields f;
+    f.solid = const_cast<uint8_t*>(d_solid);  // only read
+    auto pick = [&](auto* given, const char* tag, size_t bytes) {
+        using T = std::remove_pointer_t<decltype(given)>;
+        return given ? given : static_cast<T*>(ctx->scratch(tag, bytes));
+    };
+    if (o.run_pores) {
+        f.edt2 = pick(out->edt2, "pipe.edt2", n * 4);
+        f.crad2 = pick(out->crad2, "pipe.crad2", n * 4);
+        f.cx = pick(out->cx, "pipe.cx", n * 4);
+        f.cy = pick(out->cy, "pipe.cy", n * 4);
+        f.cz = pick(out->cz, "pipe.cz", n * 4);
+        f.mask = pick(out->maxball_mask, "pipe.mask", n);
+        f.labels = pick(out->pore_labels, "pipe.labels", n * 4);
+        f.labels_ws = pick(out->watershed_labels, "pipe.labels_ws", n * 4);
+    }
+    if (o.run_geodesic) {
+        f.cavity = pick(out->cavity, "pipe.cavity", n * 4);
+        if (geo64) f.dist64 = pick(out->dist_f64, "pipe.dist64", n * 8);
+        else f.dist32 = pick(out->dist_f32, "pipe.dist32", n * 4);
+    }
+    run_chain(ctx, f, dims, o, out);
+    ctx->sync();
+}
+
+}  // namespace pma
+
 extern "C" int pma_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims,
                                  const pma_options* opts, pma_outputs* out) {
     return guarded([&] {
-        PMA_REQUIRE(ctx && h_solid && out, PMA_ERR_ARGUMENT, "pma_pipeline_host: null argument");
-        pma::check_dims(dims);
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "pma_pipeline_host: null context");
         PMA_CUDA(cudaSetDevice(ctx->device));
-        pma_options o{PMA_D3Q27, 1, 1, 0};
-        if (opts) o = *opts;
-        const size_t n = pma::voxels(dims);
-        const bool geo64 = o.run_geodesic && o.geodesic_fp64;
-        pma::Fields f = pma::alloc_fields(ctx, n, o.run_pores != 0, o.run_geodesic != 0 && !geo64, geo64);
-        if (geo64) f.cavity = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
-        PMA_CUDA(cudaMemcpyAsync(f.solid, h_solid, n, cudaMemcpyHostToDevice, ctx->stream));
-        out->pores = nullptr;
-        out->watershed = nullptr;
-        out->n_cavities = 0;
-        if (o.run_pores) {
-            pma::edt(ctx, f.solid, dims, f.edt2, &out->edt_stats, nullptr, 0);
-            pma::containing_balls(ctx, f.edt2, dims, out->edt_stats.max_edt2, f.crad2, f.cx, f.cy,
-                                  f.cz, f.mask, &out->maximum_balls_count);
-            out->pores = pma::pores(ctx, f.mask, f.edt2, f.crad2, dims, o.stencil, f.labels);
-            pma::remove_empty_pores(ctx, out->pores, f.labels, dims);
-            out->watershed = pma::watershed(ctx, out->pores, f.crad2, dims, o.stencil,
-                                            out->edt_stats.max_edt2, f.labels_ws);
-            pma::d2h(ctx, out->edt2, f.edt2, n);
-            pma::d2h(ctx, out->crad2, f.crad2, n);
-            pma::d2h(ctx, out->cx, f.cx, n);
-            pma::d2h(ctx, out->cy, f.cy, n);
-            pma::d2h(ctx, out->cz, f.cz, n);
-            pma::d2h(ctx, out->maxball_mask, f.mask, n);
-            pma::d2h(ctx, out->pore_labels, f.labels, n);
-            pma::d2h(ctx, out->watershed_labels, f.labels_ws, n);
-        }
-        if (o.run_geodesic && !geo64) {
-            out->n_cavities = pma::geodesic<float>(ctx, f.solid, dims, o.stencil, f.dist32, f.cavity,
-                                                   out->cavities, 16);
-            pma::d2h(ctx, out->dist_f32, f.dist32, n);
-            pma::d2h(ctx, out->cavity, f.cavity, n);
-        } else if (o.run_geodesic) {
-            out->n_cavities = pma::geodesic<double>(ctx, f.solid, dims, o.stencil, f.dist64, f.cavity,
-                                                    out->cavities, 16);
-            pma::d2h(ctx, out->dist_f64, f.dist64, n);
-            pma::d2h(ctx, out->cavity, f.cavity, n);
-        }
-        ctx->sync();
+        pma::run_pipeline_host(ctx, h_solid, dims, pma::options_or_default(opts), out);
     });
 }
 

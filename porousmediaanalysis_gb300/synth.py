@@ -142,3 +142,31 @@ def spinodal(shape=(1024, 1024, 1024), waves=1000, wavelength=48.0, porosity=0.7
     idx = torch.randint(0, out.numel(), (1 << 24,), generator=g, device=dev)
     t = torch.quantile(out.reshape(-1)[idx].double(), 1.0 - porosity).float()
     return (out <= t).to(torch.uint8)
+
+
+def sphere_pack_gpu(shape, ctx, rmin=3.0, rmax=12.0, solid_fraction=0.40, seed=4, classes=10,
+                    device="cuda"):
+    """Sphere pack for large volumes, generated on the GPU: a Boolean model whose sphere count
+    gives the expected solid fraction, with radii uniform in [rmin, rmax] quantised to
+    `classes` values. Each radius class is drawn as the voxels within r of its centres, using
+    the squared distance transform of the centre points (pma_edt). Returns a (SZ, SX, SY)
+    uint8 CUDA tensor, 1 = solid."""
+    import torch
+    from . import compute_euclidean_distances
+    sz, sx, sy = shape
+    n = sz * sx * sy
+    radii = rmin + (np.arange(classes) + 0.5) * (rmax - rmin) / classes
+    mean_volume = float(np.mean(4.0 / 3.0 * np.pi * radii ** 3))
+    density = -math.log(1.0 - solid_fraction) / mean_volume  # centres per voxel
+    rng = np.random.default_rng(seed)
+    solid = torch.zeros(shape, dtype=torch.uint8, device=device)
+    for r in radii:
+        count = int(rng.poisson(density * n / classes))
+        if count == 0:
+            continue
+        pts = torch.zeros(n, dtype=torch.uint8, device=device)
+        pts[torch.from_numpy(rng.integers(0, n, count)).to(device)] = 1
+        edt2, _, _ = compute_euclidean_distances(ctx, pts.view(shape))
+        solid |= (edt2 <= int(r * r)).to(torch.uint8)
+        del edt2, pts
+    return solid
