@@ -53,6 +53,19 @@ __global__ void fill_u32(uint32_t* __restrict__ a, size_t n, uint32_t value) {
     PMA_GRID_STRIDE(i, n) a[i] = value;
 }
 
+__global__ void flag_seeds(const uint32_t* __restrict__ seed, size_t np, uint8_t* __restrict__ flags) {
+    PMA_GRID_STRIDE(p, np) flags[p] = seed[p] != kNone;
+}
+
+// up = [seed ranks (ascending) | their pore ids]
+__global__ void scatter_seed_ids(const uint32_t* __restrict__ up, size_t npores, uint32_t* __restrict__ rank2pore,
+                                 uint32_t* __restrict__ rank2id) {
+    PMA_GRID_STRIDE(k, npores) {
+        rank2pore[up[k]] = static_cast<uint32_t>(k);
+        rank2id[up[k]] = up[npores + k];
+    }
+}
+
 __global__ void scatter_rank(const uint32_t* __restrict__ voxel_of_rank, size_t n,
                              uint32_t* __restrict__ crank) {
     PMA_GRID_STRIDE(r, n) crank[voxel_of_rank[r]] = static_cast<uint32_t>(r);
@@ -85,6 +98,9 @@ __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int
         g.coords(v, x, y, z);
         // Each unordered pair once: the 13 offsets whose linear index delta
         // dz*SX*SY + dx*SY + dy is positive, i.e. (dz, dx, dy) > 0 lexicographically.
+        // rv: a known ancestor of v (its root after the previous union), so later root walks
+        // from v start close to the root.
+        uint32_t rv = static_cast<uint32_t>(v);
         for (int k = 0; k < 13; ++k) {
             int dx, dy, dz;
             if (k < 4) {
@@ -101,7 +117,8 @@ __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int
             if (!g.inside(nx, ny, nz)) continue;
             const size_t w = g.idx(nx, ny, nz);
             if (crad[w] != r) continue;
-            uint32_t a = uf_root(parent, static_cast<uint32_t>(v));
+            if (parent[w] == rv) continue;  // already joined
+            uint32_t a = uf_root(parent, rv);
             uint32_t b = uf_root(parent, static_cast<uint32_t>(w));
             int it = 0;
             while (a != b) {
@@ -119,6 +136,7 @@ __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int
                     a = old;
                 }
             }
+            rv = a < b ? a : b;  // the surviving root, an ancestor of v
         }
     }
 }
@@ -179,12 +197,15 @@ __global__ void plateau_stats(const uint32_t* __restrict__ pid, const uint32_t* 
 }
 
 // Plateau edges q -> p (crad strictly decreasing), deduplicated per voxel.
+constexpr int kEdgeTable = 2048;  // shared-memory pair set of plateau_edges (power of two)
+
 template <bool kWrite>
 __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
                               Grid g, size_t n, int d3q7, unsigned long long* __restrict__ count,
                               unsigned long long* __restrict__ edges, unsigned long long cap) {
     unsigned long long local = 0;
     const unsigned lane = threadIdx.x & 31;
+    __shared__ unsigned long long table[kWrite ? kEdgeTable : 1];
     // block-uniform trip count, so whole warps reach the warp-wide placement below
     for (size_t base = static_cast<size_t>(blockIdx.x) * blockDim.x; base < n;
          base += static_cast<size_t>(gridDim.x) * blockDim.x) {
@@ -212,6 +233,28 @@ __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* 
             }
         }
         if (kWrite) {
+            // Neighbouring voxels mostly report the same plateau pairs: keep the first copy
+            // of each pair within the block's 256 voxels (shared-memory hash set; a pair that
+            // finds no free slot is kept too - the sort and unique that follow are exact).
+            for (int i = threadIdx.x; i < kEdgeTable; i += blockDim.x) table[i] = ~0ull;
+            __syncthreads();
+            int kept = 0;
+            for (int i = 0; i < ns; ++i) {
+                const unsigned long long key = (static_cast<unsigned long long>(seen[i]) << 32) | p;
+                unsigned h = static_cast<unsigned>((key * 0x9E3779B97F4A7C15ull) >> 40) & (kEdgeTable - 1);
+                bool fresh = true;
+                for (int probe = 0; probe < 8; ++probe, h = (h + 1) & (kEdgeTable - 1)) {
+                    const unsigned long long prev = atomicCAS(&table[h], ~0ull, key);
+                    if (prev == ~0ull) break;
+                    if (prev == key) {
+                        fresh = false;
+                        break;
+                    }
+                }
+                if (fresh) seen[kept++] = seen[i];
+            }
+            __syncthreads();
+            ns = kept;
             // one atomic per warp; lanes place their edges by a warp prefix sum
             unsigned incl = static_cast<unsigned>(ns);
             for (int o = 1; o < 32; o <<= 1) {
@@ -440,18 +483,29 @@ __global__ void level_big_degrees(PlateauSets st, size_t begin, unsigned long lo
 
 // One thread per in-edge of a big plateau (t over the concatenated edge lists, doff = the
 // exclusive scan of the in-degrees): a giant plateau with a million in-edges is spread over
-// the whole GPU instead of one block. Keys of a warp are placed with one atomic.
+// the whole GPU instead of one block. The in-edges of a block mostly belong to one plateau and
+// bring the same seeds many times, so each block keeps only the first copy of a key (shared-
+// memory hash set; a key that finds no free slot is emitted anyway, the sort and unique that
+// follow are exact). Keys of a warp are placed with one atomic.
+constexpr int kMergeTable = 2048;
+
 template <class K>
-__global__ void level_expand(PlateauSets st, size_t begin, const unsigned long long* __restrict__ doff,
-                             const unsigned long long* __restrict__ deg, unsigned long long nbig,
-                             K* __restrict__ keys, unsigned long long cap, int shift) {
-    const unsigned lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) level_expand(PlateauSets st, size_t begin,
+                                                    const unsigned long long* __restrict__ doff,
+                                                    const unsigned long long* __restrict__ deg,
+                                                    unsigned long long nbig, K* __restrict__ keys,
+                                                    unsigned long long cap, int shift) {
+    __shared__ K table[kMergeTable];
+    const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
     const unsigned long long total = doff[nbig - 1] + deg[nbig - 1];
     const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
-    // warp-uniform trip count
-    for (unsigned long long t0 = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + (threadIdx.x & ~31u);
-         t0 < total; t0 += stride) {
-        const unsigned long long t = t0 + lane;
+    const K empty = ~static_cast<K>(0);
+    // block-uniform trip count (the table is cleared between rounds)
+    for (unsigned long long tb = blockIdx.x * static_cast<unsigned long long>(blockDim.x); tb < total;
+         tb += stride) {
+        for (int i = threadIdx.x; i < kMergeTable; i += blockDim.x) table[i] = empty;
+        __syncthreads();
+        const unsigned long long t = tb + threadIdx.x;
         uint32_t len = 0;
         const uint32_t* src = st.pool;
         K hi = 0;
@@ -469,16 +523,34 @@ __global__ void level_expand(PlateauSets st, size_t begin, const unsigned long l
             src = st.pool + st.soff[q];
             hi = static_cast<K>(sizeof(K) == 4 ? lo : L) << shift;
         }
-        unsigned long long incl = len;
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= static_cast<unsigned>(o)) incl += v;
+        uint32_t maxlen = len;
+        for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xFFFFFFFFu, maxlen, o));
+        for (uint32_t k = 0; k < maxlen; ++k) {
+            K key = 0;
+            bool emit = false;
+            if (k < len) {
+                key = hi | static_cast<K>(src[k]);
+                emit = true;
+                unsigned h = static_cast<unsigned>((static_cast<unsigned long long>(key) * 0x9E3779B97F4A7C15ull) >> 40) &
+                             (kMergeTable - 1);
+                for (int probe = 0; probe < 8; ++probe, h = (h + 1) & (kMergeTable - 1)) {
+                    const K prev = atomicCAS(&table[h], empty, key);
+                    if (prev == empty) break;
+                    if (prev == key) {
+                        emit = false;
+                        break;
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, emit);
+            if (!m) continue;
+            const int leader = __ffs(m) - 1;
+            unsigned long long pos = 0;
+            if (static_cast<int>(lane) == leader) pos = atomicAdd(&st.info[3], static_cast<unsigned long long>(__popc(m)));
+            pos = __shfl_sync(0xFFFFFFFFu, pos, leader) + __popc(m & lt);
+            if (emit && pos < cap) keys[pos] = key;
         }
-        unsigned long long pos = 0;
-        if (lane == 31 && incl) pos = atomicAdd(&st.info[3], incl);
-        pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + incl - len;
-        for (uint32_t k = 0; k < len; ++k)
-            if (pos + k < cap) keys[pos + k] = hi | static_cast<K>(src[k]);
+        __syncthreads();
     }
     // own seeds
     for (unsigned long long b = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; b < nbig;
@@ -774,8 +846,12 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     // Keys are (destination << 32 | source): sorting groups the predecessors of each plateau.
     int64_t ne = 0;
     if (ne_raw) {
-        sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_raw));
-        ne = unique(ctx, edges, edges_raw, static_cast<int64_t>(ne_raw), d_count);
+        unsigned long long ne_kept = 0;  // after the per-block de-duplication
+        PMA_CUDA(cudaMemcpyAsync(&ne_kept, ecount, 8, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        ne_kept = std::min(ne_kept, ne_raw);
+        sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_kept));
+        ne = unique(ctx, edges, edges_raw, static_cast<int64_t>(ne_kept), d_count);
     }
     unsigned long long* by_dst = edges_raw;
     unsigned int* eoff = buf<unsigned int>(ctx, "pores.eoff", np + 1);
@@ -884,6 +960,11 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                 int big_bits = 0;
                 while ((1ull << big_bits) < nbig) ++big_bits;
                 narrow = rank_bits < 32 && rank_bits + big_bits <= 32;
+                auto read_emitted = [&]() {
+                    PMA_CUDA(cudaMemcpyAsync(h_info, ps.info, 32, cudaMemcpyDeviceToHost, s));
+                    ctx->sync();
+                    return static_cast<int64_t>(std::min<unsigned long long>(h_info[3], total));
+                };
                 auto* deg = buf<unsigned long long>(ctx, "pores.bdeg", nbig);
                 auto* doff = buf<unsigned long long>(ctx, "pores.bdoff", nbig);
                 level_big_degrees<<<grid_for(ctx, nbig), 256, 0, s>>>(ps, b, deg);
@@ -896,8 +977,9 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                     auto* k32b = buf<uint32_t>(ctx, "pores.lkeys32b", total);
                     level_expand<uint32_t><<<eg, 256, 0, s>>>(ps, b, doff, deg, nbig, k32, total, shift);
                     ctx->check_launch("level_expand");
-                    sort_keys(ctx, k32, k32b, static_cast<int64_t>(total), rank_bits + big_bits);
-                    merged = unique(ctx, k32b, k32, static_cast<int64_t>(total), d_count);
+                    const int64_t emitted = read_emitted();
+                    sort_keys(ctx, k32, k32b, emitted, rank_bits + big_bits);
+                    merged = unique(ctx, k32b, k32, emitted, d_count);
                     keys = k32;
                     if (merged) {
                         level_runs<uint32_t><<<grid_for(ctx, merged), 256, 0, s>>>(k32, merged, ps, shift);
@@ -908,10 +990,11 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                     auto* k64b = buf<unsigned long long>(ctx, "pores.lkeys2", total);
                     level_expand<unsigned long long><<<eg, 256, 0, s>>>(ps, b, doff, deg, nbig, k64, total, shift);
                     ctx->check_launch("level_expand");
+                    const int64_t emitted = read_emitted();
                     int bits = 32;
                     while (bits < 64 && (1ull << (bits - 32)) < e - b) ++bits;
-                    sort_keys(ctx, k64, k64b, static_cast<int64_t>(total), bits);
-                    merged = unique(ctx, k64b, k64, static_cast<int64_t>(total), d_count);
+                    sort_keys(ctx, k64, k64b, emitted, bits);
+                    merged = unique(ctx, k64b, k64, emitted, d_count);
                     keys = k64;
                     if (merged) {
                         level_runs<unsigned long long><<<grid_for(ctx, merged), 256, 0, s>>>(k64, merged, ps, shift);
@@ -949,24 +1032,39 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
 
     // Seeds -> pores in rank order.
     KernelTimer kt_tables(ctx, "pores_tables");
-    std::vector<uint32_t> h_seed(np);
-    if (np) PMA_CUDA(cudaMemcpyAsync(h_seed.data(), ps.seed, np * 4, cudaMemcpyDeviceToHost, s));
-    ctx->sync();
+    // the seeds' ball ranks, compacted on the device (a few thousand of up to 10^8 plateaus)
     std::vector<uint32_t> seed_ranks;
-    for (int64_t p = 0; p < np; ++p)
-        if (h_seed[p] != kNone) seed_ranks.push_back(h_seed[p]);
+    if (np) {
+        flag_seeds<<<grid_for(ctx, np), 256, 0, s>>>(ps.seed, np, flags);
+        ctx->check_launch("flag_seeds");
+        uint32_t* d_seeds = buf<uint32_t>(ctx, "pores.seed_ranks", np);
+        const int64_t ns = select_flagged(ctx, ps.seed, flags, d_seeds, np, d_count);
+        seed_ranks.resize(ns);
+        if (ns) PMA_CUDA(cudaMemcpyAsync(seed_ranks.data(), d_seeds, ns * 4, cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+    }
     std::sort(seed_ranks.begin(), seed_ranks.end());
     const size_t npores = seed_ranks.size();
     const std::vector<uint32_t> ids = pore_id_sequence(npores);
-    std::vector<uint32_t> rank2pore(std::max<int64_t>(nb, 1), kNone), rank2id(std::max<int64_t>(nb, 1), 0);
-    for (size_t k = 0; k < npores; ++k) {
-        rank2pore[seed_ranks[k]] = static_cast<uint32_t>(k);
-        rank2id[seed_ranks[k]] = ids[k];
+    auto id_of_rank = [&](uint32_t r) {
+        return ids[std::lower_bound(seed_ranks.begin(), seed_ranks.end(), r) - seed_ranks.begin()];
+    };
+    // rank -> pore index and rank -> pore id tables on the device
+    const size_t nrank = std::max<int64_t>(nb, 1);
+    uint32_t* d_rank2pore = buf<uint32_t>(ctx, "pores.rank2pore", nrank);
+    uint32_t* d_rank2id = buf<uint32_t>(ctx, "pores.rank2id", nrank);
+    fill_u32<<<grid_for(ctx, nrank), 256, 0, s>>>(d_rank2pore, nrank, kNone);
+    ctx->check_launch("fill_u32");
+    PMA_CUDA(cudaMemsetAsync(d_rank2id, 0, nrank * 4, s));
+    if (npores) {
+        std::vector<uint32_t> up(2 * npores);
+        std::copy(seed_ranks.begin(), seed_ranks.end(), up.begin());
+        std::copy(ids.begin(), ids.end(), up.begin() + npores);
+        uint32_t* d_up = buf<uint32_t>(ctx, "pores.seed_up", up.size());
+        PMA_CUDA(cudaMemcpyAsync(d_up, up.data(), up.size() * 4, cudaMemcpyHostToDevice, s));
+        scatter_seed_ids<<<grid_for(ctx, npores), 256, 0, s>>>(d_up, npores, d_rank2pore, d_rank2id);
+        ctx->check_launch("scatter_seed_ids");
     }
-    uint32_t* d_rank2pore = buf<uint32_t>(ctx, "pores.rank2pore", rank2pore.size());
-    uint32_t* d_rank2id = buf<uint32_t>(ctx, "pores.rank2id", rank2id.size());
-    PMA_CUDA(cudaMemcpyAsync(d_rank2pore, rank2pore.data(), rank2pore.size() * 4, cudaMemcpyHostToDevice, s));
-    PMA_CUDA(cudaMemcpyAsync(d_rank2id, rank2id.data(), rank2id.size() * 4, cudaMemcpyHostToDevice, s));
     PoreAcc pa;
     pa.rank2pore = d_rank2pore;
     pa.pvol = buf<unsigned long long>(ctx, "pores.pvol", npores);
@@ -1121,9 +1219,9 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         const uint32_t* L = flat.data() + roff[gi];
         const size_t nl = roff[gi + 1] - roff[gi];
         th.n_pores = static_cast<uint32_t>(nl);
-        t->pool.push_back(rank2id[L[1]]);
-        t->pool.push_back(rank2id[L[0]]);
-        for (size_t k = 2; k < nl; ++k) t->pool.push_back(rank2id[L[k]]);
+        t->pool.push_back(id_of_rank(L[1]));
+        t->pool.push_back(id_of_rank(L[0]));
+        for (size_t k = 2; k < nl; ++k) t->pool.push_back(id_of_rank(L[k]));
         t->throats.push_back(th);
     }
     return t;
