@@ -243,9 +243,16 @@ __device__ __forceinline__ int4 decode_key(unsigned long long key, Grid g) {
                      static_cast<int>(key >> 32));
 }
 
+// 32-bit arithmetic while every offset is below 2^15 (the squared sum then fits), 64-bit
+// otherwise (only balls of radius >= 2^15, e.g. the virtual-solid distances of a long empty
+// volume).
 __device__ __forceinline__ bool covers(int4 c, int vx, int vy, int vz) {
-    const long long dx = vx - c.x, dy = vy - c.y, dz = vz - c.z;
-    return dx * dx + dy * dy + dz * dz <= static_cast<long long>(static_cast<uint32_t>(c.w));
+    const unsigned dx = static_cast<unsigned>(abs(vx - c.x)), dy = static_cast<unsigned>(abs(vy - c.y));
+    const unsigned dz = static_cast<unsigned>(abs(vz - c.z));
+    if ((dx | dy | dz) < (1u << 15)) return dx * dx + dy * dy + dz * dz <= static_cast<uint32_t>(c.w);
+    const unsigned long long d2 = static_cast<unsigned long long>(dx) * dx +
+                                  static_cast<unsigned long long>(dy) * dy + static_cast<unsigned long long>(dz) * dz;
+    return d2 <= static_cast<uint32_t>(c.w);
 }
 
 // One CTA per tile of the z-range starting at tz0: winner key of each voxel.

@@ -85,8 +85,38 @@ __device__ __forceinline__ uint32_t uf_root(uint32_t* parent, uint32_t v) {
     return cur;
 }
 
-__global__ void uf_init(const uint32_t* __restrict__ crad, size_t n, uint32_t* __restrict__ parent) {
-    PMA_GRID_STRIDE(v, n) parent[v] = crad[v] ? static_cast<uint32_t>(v) : kNone;
+// Start every void voxel under its smallest-index equal-crad neighbour (the backward
+// offsets, most negative index first), so that most trees exist before any union runs.
+__global__ void uf_init(const uint32_t* __restrict__ crad, Grid g, size_t n, int d3q7,
+                        uint32_t* __restrict__ parent) {
+    PMA_GRID_STRIDE(v, n) {
+        const uint32_t r = crad[v];
+        if (!r) {
+            parent[v] = kNone;
+            continue;
+        }
+        int x, y, z;
+        g.coords(v, x, y, z);
+        uint32_t p = static_cast<uint32_t>(v);
+        for (int k = 12; k >= 0 && p == v; --k) {  // the 13 forward offsets, negated, largest first
+            int dx, dy, dz;
+            if (k < 4) {
+                dz = 0;
+                dx = (k == 0) ? 0 : 1;
+                dy = (k == 0) ? 1 : k - 2;
+            } else {
+                dz = 1;
+                dx = (k - 4) / 3 - 1;
+                dy = (k - 4) % 3 - 1;
+            }
+            if (d3q7 && (dx != 0) + (dy != 0) + (dz != 0) > 1) continue;
+            const int nx = x - dx, ny = y - dy, nz = z - dz;
+            if (!g.inside(nx, ny, nz)) continue;
+            const size_t w = g.idx(nx, ny, nz);
+            if (crad[w] == r) p = static_cast<uint32_t>(w);
+        }
+        parent[v] = p;
+    }
 }
 
 __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int d3q7,
@@ -805,7 +835,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
 
     // Plateaus: connected sets of equal crad under the stencil.
     uint32_t* pid = buf<uint32_t>(ctx, "pores.pid", n);  // root voxel, then plateau id
-    uf_init<<<G, 256, 0, s>>>(crad2, n, pid);
+    uf_init<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid);
     ctx->check_launch("uf_init");
     {
         KernelTimer kt(ctx, "uf_hook");
