@@ -40,6 +40,13 @@ WORKLOADS = {
                      desc="128^3 union of 300 spheres, radii U[5,10]"),
 }
 
+# DRAM bytes per voxel measured by ncu over all launches of a kernel in one step of a 320^3
+# GRF (profiles/), used as the roofline's `traffic` when that kernel dominates.
+TRAFFIC_PER_VOXEL = {
+    "ws_generations": (491.0, "ncu dram__bytes_read+write of all ws_generations launches of one 320^3 "
+                              "GRF step (profiles/ws_generations_grf320.md), scaled by voxels"),
+}
+
 # Algorithmic HBM bytes per voxel of the timed kernels (reads + writes each kernel must do).
 ALGO_BYTES = {
     "edt_pass_x": 5.0,          # 1 B mask read + 4 B write
@@ -453,8 +460,14 @@ def main():
     units_per_launch = nvox * args.steps / max(nlaunch, 1)
     algo = ALGO_BYTES.get(name, 0.0) * units_per_launch
     achieved = algo / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic, traffic_src = None, None
+    if name in TRAFFIC_PER_VOXEL:
+        traffic = TRAFFIC_PER_VOXEL[name][0] * units_per_launch
+        traffic_src = TRAFFIC_PER_VOXEL[name][1]
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                "traffic_unit": "bytes per launch", "traffic_source": traffic_src,
+                "algorithmic_bytes_per_launch": algo,
                 "kernel_ms_per_step": tot_ms / args.steps,
                 "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(kern.items())}}
 

@@ -863,7 +863,10 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     auto kt_edges = std::make_unique<KernelTimer>(ctx, "plateau_edges");
     auto* ecount = reinterpret_cast<unsigned long long*>(d_count + 1);
     PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
-    plateau_edges<false><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, nullptr, 0);
+    {
+        KernelTimer kt(ctx, "edges_count");
+        plateau_edges<false><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, nullptr, 0);
+    }
     ctx->check_launch("plateau_edges(count)");
     unsigned long long ne_raw = 0;
     PMA_CUDA(cudaMemcpyAsync(&ne_raw, ecount, 8, cudaMemcpyDeviceToHost, s));
@@ -871,7 +874,10 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     auto* edges_raw = buf<unsigned long long>(ctx, "pores.edges_raw", ne_raw);
     auto* edges = buf<unsigned long long>(ctx, "pores.edges", ne_raw);
     PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
-    plateau_edges<true><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, edges_raw, ne_raw);
+    {
+        KernelTimer kt(ctx, "edges_write");
+        plateau_edges<true><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, edges_raw, ne_raw);
+    }
     ctx->check_launch("plateau_edges(write)");
     // Keys are (destination << 32 | source): sorting groups the predecessors of each plateau.
     int64_t ne = 0;

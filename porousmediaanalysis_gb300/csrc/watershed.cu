@@ -169,82 +169,61 @@ __device__ __noinline__ void ws_extend(uint32_t* ext, unsigned int* ext_count, u
 // All generations of a launch run in one kernel (see ws_generations), so data written by
 // other blocks earlier in the launch is read with __ldcg (L2, not a possibly stale L1 line);
 // only the radii, which never change, go through the read-only path.
+// ws_touch_event returns true when phase 1 stamps a same-depth claim (a node of the next
+// generation).
 template <int kPhase>
-__device__ __forceinline__ void ws_touch(const WsState& s, const uint32_t* gv, const uint32_t* gp,
-                                         unsigned long long nev, uint32_t depth, unsigned long long gen,
-                                         unsigned long long tid, unsigned long long stride) {
-    const unsigned long long tag = kMaxGen - gen;
-    for (unsigned long long seq = tid; seq < nev; seq += stride) {
-        const unsigned long long i = seq / 27;
-        const int j = static_cast<int>(seq - i * 27);
-        int dx, dy, dz;
-        if (!stencil_offset(j, s.d3q7, dx, dy, dz)) continue;
-        const uint32_t v = __ldcg(gv + i);
-        const uint32_t pore = __ldcg(gp + i);
-        int x, y, z;
-        s.g.coords(v, x, y, z);
-        const int nx = x + dx, ny = y + dy, nz = z + dz;
-        if (!s.g.inside(nx, ny, nz)) {  // WC.cpp:140-144
-            if (kPhase == 0) s.pbound[pore] = 1;
-            continue;
-        }
-        const size_t w = s.g.idx(nx, ny, nz);
-        const uint32_t r = __ldg(s.crad + w);
-        if (r == 0 || r > depth) continue;  // WC.cpp:152-156
-        if (kPhase == 0) {
-            if (__ldcg(s.claim + w) == 0) atomicMin(&s.ckey[w], (tag << 40) | seq);
-            continue;
-        }
-        const unsigned long long k = __ldcg(s.ckey + w);
-        uint32_t owner;
-        if ((k >> 40) == tag) {  // unclaimed when this generation started
-            const unsigned long long wseq = k & kSeqMask;
-            if (wseq == seq) {
-                s.claim[w] = pore + 1;
-                if (r == depth) {
-                    s.slot_voxel[seq] = static_cast<uint32_t>(w);
-                    s.slot_gen[seq] = static_cast<uint32_t>(gen);
-                } else {
-                    const unsigned pos = atomicAdd(&s.bfill[r], 1u);
-                    const unsigned long long at = s.boff[r] + pos;
-                    s.ent_time[at] = (gen << 40) | seq;
-                    s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
-                }
-                continue;
-            }
-            owner = __ldcg(gp + wseq / 27);
-        } else {
-            owner = __ldcg(s.claim + w) - 1;
-        }
-        if (owner == pore) continue;
-        ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
+__device__ __forceinline__ bool ws_touch_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
+                                               unsigned long long seq, uint32_t depth, unsigned long long gen,
+                                               unsigned long long tag) {
+    const unsigned long long i = seq / 27;
+    const int j = static_cast<int>(seq - i * 27);
+    int dx, dy, dz;
+    if (!stencil_offset(j, s.d3q7, dx, dy, dz)) return false;
+    const uint32_t v = __ldcg(gv + i);
+    const uint32_t pore = __ldcg(gp + i);
+    int x, y, z;
+    s.g.coords(v, x, y, z);
+    const int nx = x + dx, ny = y + dy, nz = z + dz;
+    if (!s.g.inside(nx, ny, nz)) {  // WC.cpp:140-144
+        if (kPhase == 0) s.pbound[pore] = 1;
+        return false;
     }
+    const size_t w = s.g.idx(nx, ny, nz);
+    const uint32_t r = __ldg(s.crad + w);
+    if (r == 0 || r > depth) return false;  // WC.cpp:152-156
+    if (kPhase == 0) {
+        if (__ldcg(s.claim + w) == 0) atomicMin(&s.ckey[w], (tag << 40) | seq);
+        return false;
+    }
+    const unsigned long long k = __ldcg(s.ckey + w);
+    uint32_t owner;
+    if ((k >> 40) == tag) {  // unclaimed when this generation started
+        const unsigned long long wseq = k & kSeqMask;
+        if (wseq == seq) {
+            s.claim[w] = pore + 1;
+            if (r == depth) {
+                s.slot_voxel[seq] = static_cast<uint32_t>(w);
+                s.slot_gen[seq] = static_cast<uint32_t>(gen);
+                return true;
+            }
+            const unsigned pos = atomicAdd(&s.bfill[r], 1u);
+            const unsigned long long at = s.boff[r] + pos;
+            s.ent_time[at] = (gen << 40) | seq;
+            s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
+            return false;
+        }
+        owner = __ldcg(gp + wseq / 27);
+    } else {
+        owner = __ldcg(s.claim + w) - 1;
+    }
+    if (owner != pore)
+        ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
+    return false;
 }
 
 // Ordered compaction of a generation's same-depth claims (event slots stamped with the
-// generation number), in three steps: counts per chunk of kChunk slots, an exclusive scan of
-// the counts (block 0), and the scatter of the claims in event order.
-__device__ __forceinline__ void ws_slot_count(const uint32_t* slot_gen, unsigned long long nev, uint32_t gen,
-                                              unsigned int* ccount, unsigned int* part) {
-    const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
-    for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        unsigned int local = 0;
-        for (unsigned k = threadIdx.x; k < kChunk; k += blockDim.x) {
-            const unsigned long long e = c * kChunk + k;
-            local += (e < nev && __ldcg(slot_gen + e) == gen) ? 1u : 0u;
-        }
-        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
-        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = local;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned int sum = 0;
-            for (unsigned w = 0; w < blockDim.x / 32; ++w) sum += part[w];
-            ccount[c] = sum;
-        }
-        __syncthreads();
-    }
-}
-
+// generation number), in three steps: counts per chunk of kChunk slots (made by phase 1), an
+// exclusive scan of the counts (block 0), and the scatter of the claims in event order.
 __device__ __forceinline__ void ws_slot_scan(unsigned int* ccount, unsigned long long nev, unsigned int* ng_next,
                                              unsigned int* part) {
     const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
@@ -345,11 +324,28 @@ __global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t
         const uint32_t* gp = cur ? gp1 : gp0;
         uint32_t* nv = cur ? gv0 : gv1;
         uint32_t* np_ = cur ? gp0 : gp1;
-        ws_touch<0>(s, gv, gp, nev, depth, gen, tid, stride);
+        const unsigned long long tag = kMaxGen - gen;
+        for (unsigned long long seq = tid; seq < nev; seq += stride) ws_touch_event<0>(s, gv, gp, seq, depth, gen, tag);
         grid.sync();
-        ws_touch<1>(s, gv, gp, nev, depth, gen, tid, stride);
-        grid.sync();
-        ws_slot_count(s.slot_gen, nev, static_cast<uint32_t>(gen), ccount, part);
+        // Phase 1 by chunks of kChunk events (4 per thread), so that each block also counts
+        // its chunk's same-depth claims for the compaction.
+        const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
+        for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
+            unsigned int local = 0;
+            for (int k = 0; k < 4; ++k) {
+                const unsigned long long seq = c * kChunk + k * (kChunk / 4) + threadIdx.x;
+                if (seq < nev && ws_touch_event<1>(s, gv, gp, seq, depth, gen, tag)) ++local;
+            }
+            for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
+            if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = local;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned int sum = 0;
+                for (unsigned w = 0; w < blockDim.x / 32; ++w) sum += part[w];
+                ccount[c] = sum;
+            }
+            __syncthreads();
+        }
         grid.sync();
         if (blockIdx.x == 0) ws_slot_scan(ccount, nev, ng + (cur ^ 1), part);
         grid.sync();
