@@ -134,6 +134,22 @@ def device_step(pma, ctx, solid):
                 ws_throats=ws_table.counts()[1], cavities=len(cavities))
 
 
+def replica_max(x, world, device):
+    """The slowest rank's time: every rank runs its own replica, and the job ends with the last."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(voxels_per_rank, steps, world, seconds):
+    """Whole-job Gvoxel/s of `world` replicas that each processed `steps` volumes."""
+    return world * voxels_per_rank * steps / seconds / 1e9
+
+
 def batch_volumes(count=256, seed=4):
     """The 256-volume batch: axis lengths log-uniform in [32, 192], sphere packs with radii
     U[3, 12] added until the solid fraction reaches 0.40."""
@@ -417,11 +433,8 @@ def main():
     ms = start.elapsed_time(stop)
     kern = ctx.timing_report()
     ctx.set_timing(False)
-    t = torch.tensor([ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * nvox * args.steps / (ms_max / 1e3) / 1e9
+    ms_max = replica_max(ms, world, dev)
+    value = replica_throughput(nvox, args.steps, world, ms_max / 1e3)
 
     # End-to-end through the C ABI with pinned host buffers.
     import numpy as np
@@ -440,10 +453,7 @@ def main():
                           out_arrays=outs)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], device=dev)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * nvox * args.steps / float(te.item()) / 1e9
+    e2e_value = replica_throughput(nvox, args.steps, world, replica_max(e2e_s, world, dev))
 
     # Roofline of the dominant timed kernel.
     peaks = {}

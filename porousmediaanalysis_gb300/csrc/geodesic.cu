@@ -10,9 +10,11 @@
 // Bucketing: all step weights w are >= 1 (1, sqrt 2, sqrt 3, or 1 for D3Q7) and in
 // round-to-nearest fl(d + w) >= floor(d) + 1, so relaxing a voxel of bucket floor(d) = k
 // only reaches buckets k+1 and k+2. Bucket k is therefore final when it is processed and
-// one parallel sweep per bucket suffices (Dial's algorithm). Buckets live in a ring of
-// four voxel lists; a per-voxel mark (the lowest bucket appended to) keeps a voxel at most
-// once in each bucket list.
+// one parallel sweep per bucket suffices (Dial's algorithm). Buckets are a ring of four
+// bitmaps over the voxels (a voxel is set in bucket b's bitmap when its distance drops into
+// b); before its sweep, bucket k's bitmap is compacted into a list in voxel order (per block
+// of 8192 voxels), which is also cleared for bucket k + 4. A voxel whose distance dropped to a
+// lower bucket after being set is skipped as stale.
 #include "pma_internal.h"
 
 #include <cfloat>
@@ -48,9 +50,12 @@ struct Geo {
 };
 
 struct Frontier {
-    uint32_t* lists;       // four bucket lists of cap entries each: bucket b uses list b & 3
-    unsigned int* count;   // [4]
-    uint32_t cap;
+    uint32_t* bits;        // four bitmaps of nwords words: bucket b uses bitmap b & 3
+    size_t nwords;
+    unsigned int* count;   // [4] voxels set in each bitmap
+    uint32_t* list;        // the compacted bucket being swept
+    unsigned int* list_n;  // its length
+    uint32_t cap;          // list capacity
     unsigned int* overflow;
     unsigned long long* settled;  // voxels settled in this cavity
     unsigned int* walls;          // bit 2i: plane axis i at 0, bit 2i+1: at size-1
@@ -58,51 +63,82 @@ struct Frontier {
 
 template <class T>
 __global__ void geo_init(const uint8_t* __restrict__ solid, size_t n, T* __restrict__ dist,
-                         uint32_t* __restrict__ cavity, int* __restrict__ mark) {
+                         uint32_t* __restrict__ cavity) {
     for (size_t v = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; v < n;
          v += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const bool s = solid[v] != 0;  // SPC.cpp:354-372
         dist[v] = s ? static_cast<T>(-1) : Bits<T>::unknown();
         cavity[v] = s ? 0u : 0xFFFFFFFFu;
-        mark[v] = 0x7FFFFFFF;
     }
 }
 
 template <class T>
-__device__ __forceinline__ void enqueue(const Frontier& f, int* mark, uint32_t v, T d) {
-    // A voxel's bucket only decreases; the mark keeps the lowest bucket it was appended to,
-    // so each bucket list holds a voxel at most once even when improvements race.
-    const int b = Bits<T>::bucket(d);
-    if (atomicMin(&mark[v], b) <= b) return;
-    const unsigned pos = atomicAdd(&f.count[b & 3], 1u);
-    if (pos < f.cap) f.lists[static_cast<size_t>(b & 3) * f.cap + pos] = v;
-    else atomicExch(f.overflow, 1u);
+__global__ void geo_start(Frontier f, T* dist, uint32_t v) {
+    dist[v] = static_cast<T>(0);
+    f.bits[v >> 5] |= 1u << (v & 31);  // bucket 0
+    f.count[0] = 1;
 }
 
-template <class T>
-__global__ void geo_start(Frontier f, int* mark, T* dist, uint32_t v) {
-    dist[v] = static_cast<T>(0);
-    enqueue<T>(f, mark, v, static_cast<T>(0));
+// Bucket k's bitmap -> list (voxel order within each block's 8192 voxels), cleared behind.
+__global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
+    __shared__ unsigned int wsum[8];
+    __shared__ unsigned int base;
+    uint32_t* bm = f.bits + static_cast<size_t>(k & 3) * f.nwords;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (size_t w0 = static_cast<size_t>(blockIdx.x) * blockDim.x; w0 < f.nwords;
+         w0 += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t w = w0 + threadIdx.x;
+        uint32_t word = 0;
+        if (w < f.nwords) {
+            word = bm[w];
+            if (word) bm[w] = 0;
+        }
+        const unsigned c = __popc(word);
+        unsigned incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<unsigned>(o)) incl += t;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int i = 0; i < 8; ++i) {
+                const unsigned v = wsum[i];
+                wsum[i] = tot;
+                tot += v;
+            }
+            base = tot ? atomicAdd(f.list_n, tot) : 0u;
+        }
+        __syncthreads();
+        unsigned pos = base + wsum[warp] + incl - c;
+        while (word) {
+            const int bit = __ffs(word) - 1;
+            word &= word - 1;
+            if (pos < f.cap) f.list[pos] = static_cast<uint32_t>(w * 32 + bit);
+            else atomicExch(f.overflow, 1u);
+            ++pos;
+        }
+        __syncthreads();
+    }
 }
 
 // Processes bucket k: settle its voxels and relax their neighbours. One thread per
 // (entry, stencil position): the wavefront of a bucket is a thin shell of a few thousand to a
 // few hundred thousand voxels, and 27 threads per voxel keep enough loads in flight to hide
-// their latency; the neighbours of one voxel fall in one warp and share cache lines.
-// The mark makes every voxel appear at most once in a bucket's list, so a live entry
-// (bucket(dist) == k) is settled exactly once, by its centre thread.
+// their latency; the neighbours of one voxel fall in one warp and share cache lines, and the
+// list is in voxel order, so neighbouring warps share them too. Each voxel is in the list
+// once, so a live entry (bucket(dist) == k) is settled exactly once, by its centre thread.
 template <class T>
-__global__ void geo_bucket(const uint8_t* __restrict__ solid, Geo g, int d3q7, T w1, T w2, T w3,
-                           T* __restrict__ dist, uint32_t* __restrict__ cavity, int* __restrict__ mark,
-                           Frontier f, int k, uint32_t cavity_id) {
+__global__ void geo_bucket(Geo g, int d3q7, T w1, T w2, T w3, T* __restrict__ dist,
+                           uint32_t* __restrict__ cavity, Frontier f, int k, uint32_t cavity_id) {
     typedef typename Bits<T>::U U;
-    if (blockIdx.x == 0 && threadIdx.x == 0) f.count[(k + 3) & 3] = 0;  // list of bucket k-1
-    const unsigned n = min(f.count[k & 3], f.cap);
-    const uint32_t* list = f.lists + static_cast<size_t>(k & 3) * f.cap;
+    const unsigned n = min(*f.list_n, f.cap);
+    const uint32_t* list = f.list;
     unsigned long long my_settled = 0;
     unsigned my_walls = 0;
     const unsigned long long total = static_cast<unsigned long long>(n) * 27;
-    const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+    const unsigned lane = threadIdx.x & 31;
     for (unsigned long long t = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; t < total;
          t += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
         const unsigned i = static_cast<unsigned>(t / 27);
@@ -140,37 +176,22 @@ __global__ void geo_bucket(const uint8_t* __restrict__ solid, Geo g, int d3q7, T
                     if (nd < dist[w]) {
                         const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
                         if (Bits<T>::to(nd) < old) {
-                            // a voxel's bucket only decreases; the mark keeps the lowest bucket
-                            // it was appended to, so each list holds it at most once
                             pb = Bits<T>::bucket(nd);
-                            push = atomicMin(&mark[w], pb) > pb;
+                            const uint32_t bit = 1u << (w & 31);
+                            push = !(atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit) & bit);
                         }
                     }
                 }
             }
         }
-        // Appends, one counter update per warp and target list: relaxations from bucket k
-        // reach buckets k + 1 and k + 2 only (steps are in [1, 2)).
+        // newly set bits, counted per warp and target bitmap (buckets k + 1 and k + 2 only:
+        // steps are in [1, 2))
         const unsigned active = __activemask();
         for (int tb = 1; tb <= 2; ++tb) {
-            const bool mine = push && pb == k + tb;
-            const unsigned m = __ballot_sync(active, mine);
-            if (!m) continue;
-            const int leader = __ffs(m) - 1;
-            unsigned base = 0;
-            if (static_cast<int>(lane) == leader) base = atomicAdd(&f.count[(k + tb) & 3], static_cast<unsigned>(__popc(m)));
-            base = __shfl_sync(active, base, leader);
-            if (mine) {
-                const unsigned pos = base + __popc(m & lt);
-                if (pos < f.cap) f.lists[static_cast<size_t>((k + tb) & 3) * f.cap + pos] = static_cast<uint32_t>(w);
-                else atomicExch(f.overflow, 1u);
-            }
+            const unsigned m = __ballot_sync(active, push && pb == k + tb);
+            if (m && static_cast<int>(lane) == __ffs(m) - 1) atomicAdd(&f.count[(k + tb) & 3], static_cast<unsigned>(__popc(m)));
         }
-        if (push && (pb < k + 1 || pb > k + 2)) {  // not reachable with steps in [1, 2)
-            const unsigned pos = atomicAdd(&f.count[pb & 3], 1u);
-            if (pos < f.cap) f.lists[static_cast<size_t>(pb & 3) * f.cap + pos] = static_cast<uint32_t>(w);
-            else atomicExch(f.overflow, 1u);
-        }
+        if (push && (pb < k + 1 || pb > k + 2)) atomicAdd(&f.count[pb & 3], 1u);  // not reachable
     }
     for (int o = 16; o > 0; o >>= 1) {
         my_settled += __shfl_xor_sync(0xFFFFFFFFu, my_settled, o);
@@ -180,6 +201,12 @@ __global__ void geo_bucket(const uint8_t* __restrict__ solid, Geo g, int d3q7, T
         if (my_settled) atomicAdd(f.settled, my_settled);
         if (my_walls) atomicOr(f.walls, my_walls);
     }
+}
+
+// Before bucket k is compacted: empty the list and its bitmap count.
+__global__ void geo_next(Frontier f, int k) {
+    *f.list_n = 0;
+    f.count[k & 3] = 0;
 }
 
 // Start-voxel search on box shells h0 .. h0+nh-1 around the centre, in the reference's
@@ -235,19 +262,24 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
     const unsigned grid = static_cast<unsigned>(std::min<size_t>(div_up(n, 256), ctx->num_sms * 16ull));
 
     const uint32_t cap = static_cast<uint32_t>(std::min<size_t>(n, size_t(1) << 28));
-    int* mark = static_cast<int*>(ctx->scratch("geo.mark", n * 4));
-    auto* lists = static_cast<uint32_t*>(ctx->scratch("geo.lists", 4ull * cap * 4));
+    const size_t nwords = (n + 31) / 32;
+    auto* bits = static_cast<uint32_t*>(ctx->scratch("geo.bits", 4 * nwords * 4));
+    auto* list = static_cast<uint32_t*>(ctx->scratch("geo.list", static_cast<size_t>(cap) * 4));
     auto* misc = static_cast<unsigned long long*>(ctx->scratch("geo.misc", 64));
     Frontier f;
-    f.lists = lists;
+    f.bits = bits;
+    f.nwords = nwords;
+    f.list = list;
     f.count = reinterpret_cast<unsigned int*>(misc);          // 4 x u32 = misc[0..1]
     f.overflow = reinterpret_cast<unsigned int*>(misc + 2);   // misc[2] low
     f.walls = reinterpret_cast<unsigned int*>(misc + 3);      // misc[3] low
     f.settled = misc + 4;
     unsigned long long* best = misc + 5;
+    f.list_n = reinterpret_cast<unsigned int*>(misc + 6);     // misc[6] low
     f.cap = cap;
+    PMA_CUDA(cudaMemsetAsync(bits, 0, 4 * nwords * 4, s));
 
-    geo_init<T><<<grid, 256, 0, s>>>(solid, n, dist, cavity, mark);
+    geo_init<T><<<grid, 256, 0, s>>>(solid, n, dist, cavity);
     ctx->check_launch("geo_init");
 
     // SPC.cpp:443-458: centre = round(size * 0.5) clipped to size - 1.
@@ -265,6 +297,7 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
     int ncav = 0;
     const int max_buckets_per_sync = 32;
     const unsigned bucket_grid = static_cast<unsigned>(ctx->num_sms * 8);
+    const unsigned compact_grid = static_cast<unsigned>(std::min<size_t>(div_up(nwords, 256), ctx->num_sms * 8ull));
     while (true) {  // SPC.cpp:94-140
         ++half;
         // SelectStartingPosition (SPC.cpp:396-426)
@@ -324,16 +357,17 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
         cavity_id += 127;
         PMA_CUDA(cudaMemsetAsync(misc, 0, 5 * 8, s));  // counts, overflow, walls, settled
         const size_t sidx = (static_cast<size_t>(start[2]) * d.sx + start[0]) * d.sy + start[1];
-        geo_start<T><<<1, 1, 0, s>>>(f, mark, dist, static_cast<uint32_t>(sidx));
+        geo_start<T><<<1, 1, 0, s>>>(f, dist, static_cast<uint32_t>(sidx));
         ctx->check_launch("geo_start");
         int k = 0;
         while (true) {
             KernelTimer kt(ctx, "geo_bucket");
             for (int i = 0; i < max_buckets_per_sync; ++i, ++k) {
-                geo_bucket<T><<<bucket_grid, 256, 0, s>>>(solid, g, d3q7, w1, w2, w3, dist, cavity,
-                                                         mark, f, k, cavity_id);
+                geo_next<<<1, 1, 0, s>>>(f, k);
+                geo_compact<<<compact_grid, 256, 0, s>>>(f, k);
+                geo_bucket<T><<<bucket_grid, 256, 0, s>>>(g, d3q7, w1, w2, w3, dist, cavity, f, k, cavity_id);
             }
-            ctx->count_launch(max_buckets_per_sync - 1);
+            ctx->count_launch(3 * max_buckets_per_sync - 1);
             ctx->check_launch("geo_bucket");
             PMA_CUDA(cudaMemcpyAsync(h, misc, 3 * 8, cudaMemcpyDeviceToHost, s));
             ctx->sync();

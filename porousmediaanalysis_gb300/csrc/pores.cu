@@ -1113,6 +1113,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     }
 
     // Throats: plateaus with two or more seeds, grouped by equal seed sets.
+    auto kt_groups = std::make_unique<KernelTimer>(ctx, "tables_groups");
     if (np) {
         flag_multi<<<grid_for(ctx, np), 256, 0, s>>>(ps.slen, np, flags);
         ctx->check_launch("flag_multi");
@@ -1196,6 +1197,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemcpyAsync(flat.data(), d_rlist, flat.size() * 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
     }
+    kt_groups.reset();
+    auto kt_host = std::make_unique<KernelTimer>(ctx, "tables_ids");
     // Throat ids: order by (last pore of the type, first voxel), counting down from
     // UINT32_MAX - 1 (BasePoreAndThroatComputer.cpp:122-130).
     std::vector<int64_t> gorder(ngroups);
@@ -1210,6 +1213,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     group_tid = buf<uint32_t>(ctx, "pores.gtid", group_tid_h.size());
     PMA_CUDA(cudaMemcpyAsync(group_tid, group_tid_h.data(), group_tid_h.size() * 4, cudaMemcpyHostToDevice, s));
 
+    kt_host.reset();
+    auto kt_labels = std::make_unique<KernelTimer>(ctx, "tables_labels");
     // Labels.
     uint32_t* plabel = buf<uint32_t>(ctx, "pores.plabel", np);
     if (np) {
@@ -1220,6 +1225,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     voxel_labels<<<G, 256, 0, s>>>(pid, plabel, n, labels);
     ctx->check_launch("voxel_labels");
 
+    kt_labels.reset();
     // Table (pores in id order, throats in id order).
     std::vector<unsigned long long> pvol(npores);
     std::vector<unsigned int> pbound(npores);
