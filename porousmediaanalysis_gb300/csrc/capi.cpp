@@ -19,17 +19,30 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 using pma::Error;
 using pma::guarded;
 
+static cudaMemPool_t ensure_pool(pma_ctx* c) {
+    if (c->pool) return c->pool;
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = c->device;
+    PMA_CUDA(cudaMemPoolCreate(&c->pool, &props));
+    unsigned long long keep = 256ull << 20;  // freed blocks kept for reuse beyond this go back
+    PMA_CUDA(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    return c->pool;
+}
+
 void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
     Buf& b = cache[tag];
     if (b.bytes >= bytes && b.ptr) return b.ptr;
-    if (b.ptr) {
-        PMA_CUDA(cudaStreamSynchronize(stream));
-        PMA_CUDA(cudaFree(b.ptr));
+    cudaMemPool_t mp = ensure_pool(this);
+    if (b.ptr) {  // stream-ordered: freed after the work already queued on the stream
+        PMA_CUDA(cudaFreeAsync(b.ptr, stream));
         b.ptr = nullptr;
         b.bytes = 0;
     }
     size_t want = bytes < 256 ? 256 : bytes;
-    cudaError_t e = cudaMalloc(&b.ptr, want);
+    cudaError_t e = cudaMallocFromPoolAsync(&b.ptr, want, mp, stream);
     if (e != cudaSuccess) {
         b.ptr = nullptr;
         (void)cudaGetLastError();
@@ -43,8 +56,7 @@ void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
 void pma_ctx::release(const std::string& tag) {
     auto it = cache.find(tag);
     if (it == cache.end()) return;
-    PMA_CUDA(cudaStreamSynchronize(stream));
-    if (it->second.ptr) PMA_CUDA(cudaFree(it->second.ptr));
+    if (it->second.ptr) PMA_CUDA(cudaFreeAsync(it->second.ptr, stream));
     cache.erase(it);
 }
 
@@ -109,7 +121,9 @@ int pma_ctx_destroy(pma_ctx* ctx) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
         for (auto& kv : ctx->cache)
-            if (kv.second.ptr) cudaFree(kv.second.ptr);
+            if (kv.second.ptr) cudaFreeAsync(kv.second.ptr, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -120,8 +134,9 @@ int pma_ctx_set_stream(pma_ctx* ctx, void* stream) {
     return guarded([&] {
         PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
         PMA_CUDA(cudaSetDevice(ctx->device));
+        // scratch buffers are stream-ordered: finish the old stream's work before switching
+        PMA_CUDA(cudaStreamSynchronize(ctx->stream));
         if (ctx->own_stream) {
-            PMA_CUDA(cudaStreamSynchronize(ctx->stream));
             PMA_CUDA(cudaStreamDestroy(ctx->stream));
             ctx->own_stream = false;
         }
@@ -198,8 +213,10 @@ int pma_ctx_trim(pma_ctx* ctx) {
         PMA_CUDA(cudaSetDevice(ctx->device));
         PMA_CUDA(cudaStreamSynchronize(ctx->stream));
         for (auto& kv : ctx->cache)
-            if (kv.second.ptr) PMA_CUDA(cudaFree(kv.second.ptr));
+            if (kv.second.ptr) PMA_CUDA(cudaFreeAsync(kv.second.ptr, ctx->stream));
         ctx->cache.clear();
+        PMA_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (ctx->pool) PMA_CUDA(cudaMemPoolTrimTo(ctx->pool, 0));
     });
 }
 

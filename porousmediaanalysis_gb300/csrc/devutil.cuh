@@ -13,11 +13,15 @@ struct Grid {
     __host__ __device__ __forceinline__ size_t idx(int x, int y, int z) const {
         return (static_cast<size_t>(z) * SX + x) * SY + y;
     }
+    // Volumes hold fewer than 2^32 voxels, so the division runs in 32 bits (a 64-bit
+    // integer division is several times longer and dominated the index-heavy kernels).
     __host__ __device__ __forceinline__ void coords(size_t v, int& x, int& y, int& z) const {
-        y = static_cast<int>(v % SY);
-        const size_t zx = v / SY;
-        x = static_cast<int>(zx % SX);
-        z = static_cast<int>(zx / SX);
+        const uint32_t v32 = static_cast<uint32_t>(v);
+        const uint32_t zx = v32 / static_cast<uint32_t>(SY);
+        y = static_cast<int>(v32 - zx * static_cast<uint32_t>(SY));
+        const uint32_t zz = zx / static_cast<uint32_t>(SX);
+        x = static_cast<int>(zx - zz * static_cast<uint32_t>(SX));
+        z = static_cast<int>(zz);
     }
     __host__ __device__ __forceinline__ bool inside(int x, int y, int z) const {
         return x >= 0 && x < SX && y >= 0 && y < SY && z >= 0 && z < SZ;

@@ -57,7 +57,9 @@ int guarded(F&& f) {
 
 }  // namespace pma
 
-// Device buffers cached by name; grow-only until trimmed.
+// Device buffers cached by name; grow-only until trimmed. They come from a stream-ordered
+// memory pool of the context: growing one never synchronises the device, so batch lanes and
+// serving lanes do not stall each other.
 struct pma_ctx {
     int device = 0;
     int num_sms = 0;
@@ -70,6 +72,7 @@ struct pma_ctx {
         size_t bytes = 0;
     };
     std::map<std::string, Buf> cache;
+    cudaMemPool_t pool = nullptr;  // stream-ordered pool of the scratch buffers
     void* pinned = nullptr;       // small pinned host staging area
     size_t pinned_bytes = 0;
     bool timing = false;          // bracket hot kernels with events

@@ -213,16 +213,23 @@ __global__ void plateau_stats(const uint32_t* __restrict__ pid, const uint32_t* 
                               const uint32_t* __restrict__ crank, Grid g, size_t n,
                               uint32_t* __restrict__ pcrad, unsigned int* __restrict__ psize,
                               unsigned int* __restrict__ pface, uint32_t* __restrict__ pminrank) {
+    // Neighbouring voxels mostly share a plateau: lanes of a warp with the same plateau
+    // combine their updates (one atomic per plateau and warp).
+    const unsigned lane = threadIdx.x & 31;
     PMA_GRID_STRIDE(v, n) {
         const uint32_t p = pid[v];
-        if (p == kNone) continue;
-        pcrad[p] = crad[v];
-        atomicAdd(&psize[p], 1u);
         int x, y, z;
         g.coords(v, x, y, z);
-        if (g.on_face(x, y, z)) pface[p] = 1;
-        const uint32_t rk = crank[v];
-        if (rk != kNone) atomicMin(&pminrank[p], rk);
+        const unsigned face = g.on_face(x, y, z) ? 1u : 0u;
+        const uint32_t rk = p == kNone ? kNone : crank[v];
+        const unsigned peers = __match_any_sync(__activemask(), p);
+        const unsigned any_face = __reduce_or_sync(peers, face);
+        const uint32_t min_rank = __reduce_min_sync(peers, rk);
+        if (p == kNone || static_cast<int>(lane) != __ffs(peers) - 1) continue;
+        pcrad[p] = crad[v];
+        atomicAdd(&psize[p], static_cast<unsigned>(__popc(peers)));
+        if (any_face) pface[p] = 1;
+        if (min_rank != kNone) atomicMin(&pminrank[p], min_rank);
     }
 }
 
@@ -715,10 +722,17 @@ struct PoreAcc {
 __global__ void pore_accumulate(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
                                 const uint32_t* __restrict__ pool, const unsigned int* __restrict__ psize,
                                 const unsigned int* __restrict__ pface, size_t np, PoreAcc pa) {
+    const unsigned lane = threadIdx.x & 31;
     PMA_GRID_STRIDE(p, np) {
         const uint32_t n = slen[p];
         const uint32_t* s = pool + soff[p];
-        if (n == 1) atomicAdd(&pa.pvol[pa.rank2pore[s[0]]], static_cast<unsigned long long>(psize[p]));
+        // plateaus of one pore met by a warp add their sizes with one atomic
+        const uint32_t pore = n == 1 ? pa.rank2pore[s[0]] : kNone;
+        const unsigned long long size = n == 1 ? psize[p] : 0ull;
+        const unsigned peers = __match_any_sync(__activemask(), pore);
+        unsigned long long sum = 0;
+        for (unsigned m = peers; m; m &= m - 1) sum += __shfl_sync(peers, size, __ffs(m) - 1);
+        if (pore != kNone && static_cast<int>(lane) == __ffs(peers) - 1) atomicAdd(&pa.pvol[pore], sum);
         if (pface[p])
             for (uint32_t k = 0; k < n; ++k) pa.pbound[pa.rank2pore[s[k]]] = 1;
     }
@@ -767,13 +781,14 @@ __global__ void to_group_index(const uint32_t* __restrict__ excl, const uint32_t
     PMA_GRID_STRIDE(i, m) out[i] = excl[i] + start[i] - 1u;
 }
 
+// Pore ids of each group's seed list (ascending ranks give ascending ids).
 __global__ void gather_lists(const unsigned long long* __restrict__ soff, const uint32_t* __restrict__ slen,
                              const uint32_t* __restrict__ pool, const uint32_t* __restrict__ rep,
                              const unsigned long long* __restrict__ roff, size_t ng,
-                             uint32_t* __restrict__ out) {
+                             const uint32_t* __restrict__ rank2id, uint32_t* __restrict__ out) {
     PMA_GRID_STRIDE(gi, ng) {
         const uint32_t p = rep[gi];
-        for (uint32_t k = 0; k < slen[p]; ++k) out[roff[gi] + k] = pool[soff[p] + k];
+        for (uint32_t k = 0; k < slen[p]; ++k) out[roff[gi] + k] = rank2id[pool[soff[p] + k]];
     }
 }
 
@@ -1068,6 +1083,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
 
     // Seeds -> pores in rank order.
     KernelTimer kt_tables(ctx, "pores_tables");
+    auto kt_seeds = std::make_unique<KernelTimer>(ctx, "tables_seeds");
     // the seeds' ball ranks, compacted on the device (a few thousand of up to 10^8 plateaus)
     std::vector<uint32_t> seed_ranks;
     if (np) {
@@ -1082,9 +1098,6 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     std::sort(seed_ranks.begin(), seed_ranks.end());
     const size_t npores = seed_ranks.size();
     const std::vector<uint32_t> ids = pore_id_sequence(npores);
-    auto id_of_rank = [&](uint32_t r) {
-        return ids[std::lower_bound(seed_ranks.begin(), seed_ranks.end(), r) - seed_ranks.begin()];
-    };
     // rank -> pore index and rank -> pore id tables on the device
     const size_t nrank = std::max<int64_t>(nb, 1);
     uint32_t* d_rank2pore = buf<uint32_t>(ctx, "pores.rank2pore", nrank);
@@ -1112,6 +1125,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         ctx->check_launch("pore_accumulate");
     }
 
+    kt_seeds.reset();
     // Throats: plateaus with two or more seeds, grouped by equal seed sets.
     auto kt_groups = std::make_unique<KernelTimer>(ctx, "tables_groups");
     if (np) {
@@ -1128,7 +1142,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     pma_table* t = new pma_table;
     std::vector<unsigned long long> h_gvol, h_gfirst;
     std::vector<uint32_t> h_grep;
-    std::vector<uint32_t> flat;                // seed ranks of each group's list, concatenated
+    std::vector<uint32_t> flat;                // pore ids of each group's list, concatenated
     std::vector<unsigned long long> roff(1, 0);  // list offsets into flat
     int64_t ngroups = 0;
     if (nm) {
@@ -1191,7 +1205,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         uint32_t* d_rlist = buf<uint32_t>(ctx, "pores.rlist", roff[ngroups]);
         PMA_CUDA(cudaMemcpyAsync(d_roff, roff.data(), (ngroups + 1) * 8, cudaMemcpyHostToDevice, s));
         gather_lists<<<grid_for(ctx, ngroups), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, go.grep, d_roff,
-                                                            ngroups, d_rlist);
+                                                            ngroups, d_rank2id, d_rlist);
         ctx->check_launch("gather_lists");
         flat.resize(roff[ngroups]);
         PMA_CUDA(cudaMemcpyAsync(flat.data(), d_rlist, flat.size() * 4, cudaMemcpyDeviceToHost, s));
@@ -1201,13 +1215,13 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     auto kt_host = std::make_unique<KernelTimer>(ctx, "tables_ids");
     // Throat ids: order by (last pore of the type, first voxel), counting down from
     // UINT32_MAX - 1 (BasePoreAndThroatComputer.cpp:122-130).
+    // key = (last pore id << 32) | first voxel; both fit 32 bits and first voxels are distinct
+    std::vector<std::pair<unsigned long long, int64_t>> gkey(ngroups);
+    for (int64_t i = 0; i < ngroups; ++i)
+        gkey[i] = {(static_cast<unsigned long long>(flat[roff[i + 1] - 1]) << 32) | (h_gfirst[i] & 0xFFFFFFFFull), i};
+    std::sort(gkey.begin(), gkey.end());
     std::vector<int64_t> gorder(ngroups);
-    for (int64_t i = 0; i < ngroups; ++i) gorder[i] = i;
-    std::sort(gorder.begin(), gorder.end(), [&](int64_t a, int64_t b) {
-        const uint32_t la = flat[roff[a + 1] - 1], lb = flat[roff[b + 1] - 1];
-        if (la != lb) return la < lb;
-        return h_gfirst[a] < h_gfirst[b];
-    });
+    for (int64_t k = 0; k < ngroups; ++k) gorder[k] = gkey[k].second;
     group_tid_h.assign(std::max<int64_t>(ngroups, 1), 0);
     for (int64_t k = 0; k < ngroups; ++k) group_tid_h[gorder[k]] = 0xFFFFFFFFu - 1u - static_cast<uint32_t>(k);
     group_tid = buf<uint32_t>(ctx, "pores.gtid", group_tid_h.size());
@@ -1226,6 +1240,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     ctx->check_launch("voxel_labels");
 
     kt_labels.reset();
+    KernelTimer kt_rows(ctx, "tables_rows");
     // Table (pores in id order, throats in id order).
     std::vector<unsigned long long> pvol(npores);
     std::vector<unsigned int> pbound(npores);
@@ -1251,20 +1266,21 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     }
     // Throat rows: pore list in processing order [second, first, third, ...]
     // (BasePoreAndThroatComputer.cpp:338-340, 370-371), sorted by id.
-    std::vector<int64_t> by_id(ngroups);
-    for (int64_t k = 0; k < ngroups; ++k) by_id[k] = gorder[ngroups - 1 - k];
-    for (int64_t gi : by_id) {
-        pma_throat th;
+    t->throats.resize(ngroups);
+    t->pool.resize(roff[ngroups]);
+    size_t at = 0;
+    for (int64_t k = 0; k < ngroups; ++k) {
+        const int64_t gi = gorder[ngroups - 1 - k];
+        pma_throat& th = t->throats[k];
         th.id = group_tid_h[gi];
         th.volume = h_gvol[gi];
-        th.pool_offset = t->pool.size();
+        th.pool_offset = at;
         const uint32_t* L = flat.data() + roff[gi];
         const size_t nl = roff[gi + 1] - roff[gi];
         th.n_pores = static_cast<uint32_t>(nl);
-        t->pool.push_back(id_of_rank(L[1]));
-        t->pool.push_back(id_of_rank(L[0]));
-        for (size_t k = 2; k < nl; ++k) t->pool.push_back(id_of_rank(L[k]));
-        t->throats.push_back(th);
+        t->pool[at++] = L[1];
+        t->pool[at++] = L[0];
+        for (size_t j = 2; j < nl; ++j) t->pool[at++] = L[j];
     }
     return t;
 }

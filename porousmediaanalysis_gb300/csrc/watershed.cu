@@ -369,11 +369,16 @@ __global__ void ws_unpack_entries(const unsigned long long* __restrict__ val, si
 
 __global__ void ws_volumes(const uint32_t* __restrict__ claim, const uint32_t* __restrict__ ext, size_t n,
                            unsigned long long* __restrict__ pvol, uint8_t* __restrict__ shared_flag) {
+    // lanes of a warp claimed by the same pore combine their counts
+    const unsigned lane = threadIdx.x & 31;
     PMA_GRID_STRIDE(v, n) {
         const uint32_t c = claim[v];
         const bool sh = ext[v] != 0;
         shared_flag[v] = sh;
-        if (c && !sh) atomicAdd(&pvol[c - 1], 1ull);
+        const uint32_t key = (c && !sh) ? c : 0u;
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        if (key && static_cast<int>(lane) == __ffs(peers) - 1)
+            atomicAdd(&pvol[key - 1], static_cast<unsigned long long>(__popc(peers)));
     }
 }
 
@@ -784,9 +789,11 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     PMA_CUDA(cudaMemcpyAsync(h_rows.data(), rows, h_rows.size() * 4, cudaMemcpyDeviceToHost, s));
     ctx->sync();
     // ids in creation order
+    std::vector<std::pair<unsigned long long, uint32_t>> by_time(ngr);  // creation times are distinct
+    for (int64_t i = 0; i < ngr; ++i) by_time[i] = {h_gtime[i], static_cast<uint32_t>(i)};
+    std::sort(by_time.begin(), by_time.end());
     std::vector<uint32_t> order(ngr);
-    for (int64_t i = 0; i < ngr; ++i) order[i] = static_cast<uint32_t>(i);
-    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return h_gtime[a] < h_gtime[b]; });
+    for (int64_t k = 0; k < ngr; ++k) order[k] = by_time[k].second;
     std::vector<uint32_t> gid(ngr);
     for (int64_t k = 0; k < ngr; ++k) gid[order[k]] = 0xFFFFFFFFu - 1u - static_cast<uint32_t>(k);
     uint32_t* d_gid = buf<uint32_t>(ctx, "ws.gid", ngr);
@@ -795,6 +802,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ctx->check_launch("ws_shared_labels");
     ctx->sync();
     // rows in id order (ascending id = reverse creation order)
+    t->throats.reserve(ngr);
+    t->pool.reserve(static_cast<size_t>(ngr) * 3);
     for (int64_t k = ngr - 1; k >= 0; --k) {
         const uint32_t gi = order[k];
         pma_throat th;
