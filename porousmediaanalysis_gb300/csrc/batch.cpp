@@ -60,6 +60,9 @@ extern "C" int pma_pipeline_batch(pma_ctx* ctx, pma_batch_item* items, size_t n,
         if (n == 0) return;
         const size_t want = std::min<size_t>(lanes ? static_cast<size_t>(lanes) : 8, n);
         while (ctx->lanes.size() < want) ctx->lanes.push_back(pma::make_lane(ctx));
+        // several lanes: host threads sleep in their synchronisations, leaving CPU cores to
+        // each other; a single lane spins like a plain call
+        for (size_t l = 0; l < want; ++l) ctx->lanes[l]->blocking_sync = want > 1;
         // Inputs produced on the caller's stream must be complete before the lanes read them.
         PMA_CUDA(cudaStreamSynchronize(ctx->stream));
 

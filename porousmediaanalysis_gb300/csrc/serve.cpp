@@ -186,6 +186,7 @@ int pma_server_create(pma_ctx* ctx, const pma_server_config* cfg, pma_server** o
                 pma_ctx* c = nullptr;
                 PMA_REQUIRE(pma_ctx_create(ctx->device, &c) == PMA_OK, PMA_ERR_CUDA,
                             "pma_server_create: lane context");
+                c->blocking_sync = true;
                 l.ctx = c;
             }
         } catch (...) {

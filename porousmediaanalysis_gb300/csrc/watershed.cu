@@ -652,7 +652,11 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         int per_sm = 0;
         PMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_generations, kChunk / 4, 0));
         PMA_REQUIRE(per_sm > 0, PMA_ERR_CUDA, "pma_watershed: generation kernel does not fit an SM");
-        const unsigned coop_grid = static_cast<unsigned>(ctx->num_sms * std::min(per_sm, 8));
+        // sized to the largest frontier (about 16 events per thread and phase), so that the
+        // launches of small volumes leave the rest of the GPU to other streams (batch lanes)
+        const size_t coop_need = (max_events + 16 * (kChunk / 4) - 1) / (16 * (kChunk / 4));
+        const unsigned coop_grid = static_cast<unsigned>(
+            std::max<size_t>(1, std::min<size_t>(coop_need, static_cast<size_t>(ctx->num_sms) * std::min(per_sm, 8))));
         unsigned long long gen = 0;
         unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
         auto* d_out = buf<unsigned long long>(ctx, "ws.coop_out", 2);
