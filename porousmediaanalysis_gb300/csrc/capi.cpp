@@ -72,7 +72,26 @@ void* pma_ctx::host_staging(size_t bytes) {
     return pinned;
 }
 
-void pma_ctx::sync() { PMA_CUDA(cudaStreamSynchronize(stream)); }
+int64_t* pma_ctx::pinned_count() {
+    if (!count_word) {
+        void* p = nullptr;
+        PMA_CUDA(cudaMallocHost(&p, 64));
+        count_word = static_cast<int64_t*>(p);
+    }
+    return count_word;
+}
+
+void pma_ctx::sync() {
+    if (!blocking_sync) {
+        PMA_CUDA(cudaStreamSynchronize(stream));
+        return;
+    }
+    // lanes of a batch or a server: the host thread sleeps instead of spinning, leaving the
+    // CPU cores to the other lanes' host work
+    if (!sync_event) PMA_CUDA(cudaEventCreateWithFlags(&sync_event, cudaEventBlockingSync | cudaEventDisableTiming));
+    PMA_CUDA(cudaEventRecord(sync_event, stream));
+    PMA_CUDA(cudaEventSynchronize(sync_event));
+}
 
 void pma_ctx::check_launch(const char* what) {
     count_launch(1);
@@ -124,7 +143,9 @@ int pma_ctx_destroy(pma_ctx* ctx) {
             if (kv.second.ptr) cudaFreeAsync(kv.second.ptr, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
         if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+        if (ctx->sync_event) cudaEventDestroy(ctx->sync_event);
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
+        if (ctx->count_word) cudaFreeHost(ctx->count_word);
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
     });

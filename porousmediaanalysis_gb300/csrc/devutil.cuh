@@ -65,11 +65,11 @@ inline int64_t select_flagged(pma_ctx* ctx, InIt in, const uint8_t* flags, T* ou
     PMA_CUDA(cub::DeviceSelect::Flagged(nullptr, bytes, in, flags, out, d_count, n, ctx->stream));
     void* tmp = ctx->scratch("cub.tmp", bytes);
     PMA_CUDA(cub::DeviceSelect::Flagged(tmp, bytes, in, flags, out, d_count, n, ctx->stream));
-    int64_t h = 0;
-    PMA_CUDA(cudaMemcpyAsync(&h, d_count, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    int64_t* h = ctx->pinned_count();
+    PMA_CUDA(cudaMemcpyAsync(h, d_count, sizeof(*h), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     ctx->count_launch(1);
-    return h;
+    return *h;
 }
 
 template <class T>
@@ -108,11 +108,11 @@ inline int64_t unique(pma_ctx* ctx, const T* in, T* out, int64_t n, int64_t* d_c
     PMA_CUDA(cub::DeviceSelect::Unique(nullptr, bytes, in, out, d_count, n, ctx->stream));
     void* tmp = ctx->scratch("cub.tmp", bytes);
     PMA_CUDA(cub::DeviceSelect::Unique(tmp, bytes, in, out, d_count, n, ctx->stream));
-    int64_t h = 0;
-    PMA_CUDA(cudaMemcpyAsync(&h, d_count, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    int64_t* h = ctx->pinned_count();
+    PMA_CUDA(cudaMemcpyAsync(h, d_count, sizeof(*h), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     ctx->count_launch(1);
-    return h;
+    return *h;
 }
 
 inline unsigned grid_for(pma_ctx* ctx, size_t n, int threads = 256) {

@@ -73,6 +73,8 @@ struct pma_ctx {
     };
     std::map<std::string, Buf> cache;
     cudaMemPool_t pool = nullptr;  // stream-ordered pool of the scratch buffers
+    bool blocking_sync = false;    // sync() sleeps on an event instead of spinning
+    cudaEvent_t sync_event = nullptr;
     void* pinned = nullptr;       // small pinned host staging area
     size_t pinned_bytes = 0;
     bool timing = false;          // bracket hot kernels with events
@@ -86,6 +88,8 @@ struct pma_ctx {
     void* scratch(const std::string& tag, size_t bytes);
     void release(const std::string& tag);  // frees one scratch buffer (after the stream's work)
     void* host_staging(size_t bytes);
+    int64_t* pinned_count();  // a pinned word of its own for counts read back after CUB calls
+    int64_t* count_word = nullptr;
     void sync();
     void check_launch(const char* what);
     void count_launch(uint64_t n = 1) { launches.fetch_add(n, std::memory_order_relaxed); }
