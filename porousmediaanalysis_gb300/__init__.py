@@ -68,6 +68,10 @@ class Context:
     def scratch_bytes(self):
         return capi.lib().pma_ctx_scratch_bytes(self.handle)
 
+    def trim(self):
+        """Give the scratch cache (this context's and its batch lanes') back to the device."""
+        capi.check(capi.lib().pma_ctx_trim(self.handle))
+
     def set_timing(self, enable=True):
         capi.check(capi.lib().pma_ctx_set_timing(self.handle, int(enable)))
 

@@ -33,6 +33,11 @@ static cudaMemPool_t ensure_pool(pma_ctx* c) {
 }
 
 void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
+    size_t& d = demand[tag];
+    if (bytes > d) {
+        demand_bytes += bytes - d;
+        d = bytes;
+    }
     Buf& b = cache[tag];
     if (b.bytes >= bytes && b.ptr) return b.ptr;
     cudaMemPool_t mp = ensure_pool(this);

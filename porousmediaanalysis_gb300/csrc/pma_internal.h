@@ -84,6 +84,14 @@ struct pma_ctx {
     };
     std::vector<Timed> timed;
     std::vector<pma_ctx*> lanes;  // child contexts of batch calls (own stream and scratch)
+    // Demand: the largest size each named buffer was asked for since reset_demand(), summed;
+    // what one request needs, whatever earlier requests left in the cache.
+    std::map<std::string, size_t> demand;
+    size_t demand_bytes = 0;
+    void reset_demand() {
+        demand.clear();
+        demand_bytes = 0;
+    }
 
     void* scratch(const std::string& tag, size_t bytes);
     void release(const std::string& tag);  // frees one scratch buffer (after the stream's work)

@@ -611,6 +611,97 @@ __global__ void level_runs(const K* __restrict__ keys, size_t n, PlateauSets st,
     }
 }
 
+// Sort path of a level whose big unions hold few keys in all (kSmallMerge): one block expands,
+// sorts (bitonic, shared memory) and de-duplicates them, and fills cnt/first like level_runs.
+// No host round trip: the number of merged keys stays on the device (*merged).
+constexpr int kSmallMerge = 4096;
+
+__global__ void __launch_bounds__(1024) level_merge_small(PlateauSets st, size_t begin,
+                                                          unsigned long long* __restrict__ keys,
+                                                          unsigned long long* __restrict__ merged) {
+    __shared__ unsigned long long sk[kSmallMerge];
+    __shared__ unsigned int s_count;
+    __shared__ unsigned int wsum[32];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned long long nbig = st.info[1];
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    for (unsigned long long b = warp; b < nbig; b += nw) {
+        const uint32_t L = st.big_list[b];
+        const uint32_t p = st.order[begin + L];
+        const unsigned e0 = st.eoff[p], e1 = st.eoff[p + 1];
+        const unsigned long long hi = static_cast<unsigned long long>(L) << 32;
+        for (unsigned e = e0 + lane; e < e1; e += 32) {
+            const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+            const uint32_t len = st.slen[q];
+            const uint32_t* src = st.pool + st.soff[q];
+            const unsigned pos = atomicAdd(&s_count, len);
+            for (uint32_t k = 0; k < len; ++k)
+                if (pos + k < kSmallMerge) sk[pos + k] = hi | src[k];
+        }
+        if (lane == 0 && st.seed[p] != kNone) {
+            const unsigned pos = atomicAdd(&s_count, 1u);
+            if (pos < kSmallMerge) sk[pos] = hi | st.seed[p];
+        }
+    }
+    __syncthreads();
+    const unsigned n = min(s_count, static_cast<unsigned>(kSmallMerge));
+    unsigned N = 1;
+    while (N < n) N <<= 1;
+    for (unsigned i = n + threadIdx.x; i < N; i += blockDim.x) sk[i] = ~0ull;
+    __syncthreads();
+    for (unsigned k = 2; k <= N; k <<= 1)  // bitonic sort, ascending
+        for (unsigned j = k >> 1; j > 0; j >>= 1) {
+            for (unsigned i = threadIdx.x; i < N; i += blockDim.x) {
+                const unsigned q = i ^ j;
+                if (q > i) {
+                    const unsigned long long a = sk[i], c = sk[q];
+                    if (((i & k) == 0) ? (a > c) : (a < c)) {
+                        sk[i] = c;
+                        sk[q] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // first copies, compacted in order: each thread owns a contiguous run of 4 positions
+    const unsigned per = (N + blockDim.x - 1) / blockDim.x;  // <= 4
+    const unsigned i0 = threadIdx.x * per;
+    unsigned mine = 0;
+    for (unsigned t = 0; t < per; ++t) {
+        const unsigned i = i0 + t;
+        if (i < n && (i == 0 || sk[i - 1] != sk[i])) ++mine;
+    }
+    unsigned incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<unsigned>(o)) incl += v;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned run = 0;
+        for (unsigned w = 0; w < nw; ++w) {
+            const unsigned v = wsum[w];
+            wsum[w] = run;
+            run += v;
+        }
+        *merged = run;
+    }
+    __syncthreads();
+    unsigned u = wsum[warp] + incl - mine;
+    for (unsigned t = 0; t < per; ++t) {
+        const unsigned i = i0 + t;
+        if (!(i < n && (i == 0 || sk[i - 1] != sk[i]))) continue;
+        const uint32_t L = static_cast<uint32_t>(sk[i] >> 32);
+        keys[u] = sk[i];
+        // sk[i] is a first copy, so sk[i - 1] is the previous distinct key
+        if (i == 0 || static_cast<uint32_t>(sk[i - 1] >> 32) != L) st.first[L] = u;
+        atomicAdd(&st.cnt[L], 1ull);
+        ++u;
+    }
+}
+
 // Writes the small unions (recomputed) and the list offsets of all plateaus of the level.
 __global__ void level_write(PlateauSets st, size_t begin, size_t end, const unsigned long long* __restrict__ base) {
     __shared__ uint32_t wbuf[kLevelWarps][kSmallSet];
@@ -640,10 +731,12 @@ __global__ void level_write(PlateauSets st, size_t begin, size_t end, const unsi
 }
 
 template <class K>
-__global__ void level_copy_big(const K* __restrict__ keys, size_t n, PlateauSets st,
-                               const unsigned long long* __restrict__ base, int shift) {
+__global__ void level_copy_big(const K* __restrict__ keys, size_t n_host, PlateauSets st,
+                               const unsigned long long* __restrict__ base, int shift,
+                               const unsigned long long* __restrict__ n_dev) {
     const unsigned long long b0 = *base;
     const K low = (static_cast<K>(1) << shift) - 1;
+    const size_t n = n_dev ? static_cast<size_t>(*n_dev) : n_host;
     PMA_GRID_STRIDE(i, n) {
         const uint32_t L = key_plateau(st, keys[i], shift);
         const unsigned long long pos = b0 + st.off[L];
@@ -887,7 +980,6 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     PMA_CUDA(cudaMemcpyAsync(&ne_raw, ecount, 8, cudaMemcpyDeviceToHost, s));
     ctx->sync();
     auto* edges_raw = buf<unsigned long long>(ctx, "pores.edges_raw", ne_raw);
-    auto* edges = buf<unsigned long long>(ctx, "pores.edges", ne_raw);
     PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
     {
         KernelTimer kt(ctx, "edges_write");
@@ -901,6 +993,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemcpyAsync(&ne_kept, ecount, 8, cudaMemcpyDeviceToHost, s));
         ctx->sync();
         ne_kept = std::min(ne_kept, ne_raw);
+        auto* edges = buf<unsigned long long>(ctx, "pores.edges", ne_kept);
         sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_kept));
         ne = unique(ctx, edges, edges_raw, static_cast<int64_t>(ne_kept), d_count);
     }
@@ -1005,7 +1098,16 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             int shift = 32;
             void* keys = nullptr;
             bool narrow = false;
-            if (nbig) {
+            const unsigned long long* merged_dev = nullptr;  // merged count left on the device
+            if (nbig && total <= static_cast<unsigned long long>(kSmallMerge)) {
+                KernelTimer kt2(ctx, "level_merge");
+                auto* k64 = buf<unsigned long long>(ctx, "pores.lkeys", kSmallMerge);
+                merged_dev = ps.info + 3;
+                level_merge_small<<<1, 1024, 0, s>>>(ps, b, k64, ps.info + 3);
+                ctx->check_launch("level_merge_small");
+                keys = k64;
+                merged = kSmallMerge;  // upper bound for the copy launch below
+            } else if (nbig) {
                 KernelTimer kt2(ctx, "level_merge");
                 PMA_REQUIRE(total < (1ull << 40), PMA_ERR_MEMORY, "pma_pores: seed-set union too large");
                 int big_bits = 0;
@@ -1060,10 +1162,10 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             if (merged) {
                 if (narrow)
                     level_copy_big<uint32_t><<<grid_for(ctx, merged), 256, 0, s>>>(
-                        static_cast<uint32_t*>(keys), merged, ps, base, shift);
+                        static_cast<uint32_t*>(keys), merged, ps, base, shift, nullptr);
                 else
                     level_copy_big<unsigned long long><<<grid_for(ctx, merged), 256, 0, s>>>(
-                        static_cast<unsigned long long*>(keys), merged, ps, base, shift);
+                        static_cast<unsigned long long*>(keys), merged, ps, base, shift, merged_dev);
                 ctx->count_launch(1);
             }
             level_advance<<<1, 32, 0, s>>>(base, ps.off, ps.cnt, e - b);

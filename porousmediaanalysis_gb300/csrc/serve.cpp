@@ -8,8 +8,9 @@
 // the first stage to the last; only the input and the requested outputs cross the bus.
 //
 // Memory accounting. A request's footprint is estimated as bytes-per-voxel x voxels, where
-// bytes-per-voxel is the largest scratch-to-voxel ratio seen so far (the fields and work
-// buffers of every stage are linear in the voxel count). A lane keeps its scratch between
+// bytes-per-voxel is the largest ratio of a finished request's scratch demand (the sum of the
+// largest size each named buffer was asked for) to its voxel count seen so far (the fields and
+// work buffers of every stage are linear in the voxel count). A lane keeps its scratch between
 // requests; the reservation of a lane is max(its scratch, footprint of its request). A
 // request is admitted only if the lanes' reservations stay within the budget; idle lanes
 // give their scratch back first when the budget is short, and a lane whose scratch exceeds
@@ -126,6 +127,7 @@ void lane_loop(pma_server* s, size_t li) {
         s->stats.peak_reserved_bytes = std::max<uint64_t>(s->stats.peak_reserved_bytes, reserved_total(s));
         lock.unlock();
 
+        me.ctx->reset_demand();
         const int status = guarded([&] { run_pipeline_host(me.ctx, r.solid, r.dims, s->options, r.out); });
         std::string message;
         if (status != PMA_OK) {
@@ -135,7 +137,7 @@ void lane_loop(pma_server* s, size_t li) {
         }
         const double ms =
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - r.arrival).count();
-        const uint64_t used = pma_ctx_scratch_bytes(me.ctx);
+        const uint64_t used = me.ctx->demand_bytes;
 
         lock.lock();
         if (status == PMA_OK) {

@@ -359,6 +359,47 @@ __global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t
     }
 }
 
+// A small depth bucket (n <= kSmallBucket entries) sorted by time in one block and unpacked
+// into the first generation, with its size; replaces a radix sort and two more launches.
+constexpr int kSmallBucket = 2048;
+
+__global__ void __launch_bounds__(1024) ws_sort_small(const unsigned long long* __restrict__ time,
+                                                      const unsigned long long* __restrict__ val, unsigned n,
+                                                      uint32_t* __restrict__ gv, uint32_t* __restrict__ gp,
+                                                      unsigned int* __restrict__ ng) {
+    __shared__ unsigned long long st[kSmallBucket];
+    __shared__ unsigned long long sv[kSmallBucket];
+    unsigned N = 1;
+    while (N < n) N <<= 1;
+    for (unsigned i = threadIdx.x; i < N; i += blockDim.x) {
+        st[i] = i < n ? time[i] : ~0ull;
+        sv[i] = i < n ? val[i] : 0ull;
+    }
+    __syncthreads();
+    for (unsigned k = 2; k <= N; k <<= 1)  // bitonic sort by time (times are distinct)
+        for (unsigned j = k >> 1; j > 0; j >>= 1) {
+            for (unsigned i = threadIdx.x; i < N; i += blockDim.x) {
+                const unsigned q = i ^ j;
+                if (q > i) {
+                    const unsigned long long a = st[i], c = st[q];
+                    if (((i & k) == 0) ? (a > c) : (a < c)) {
+                        st[i] = c;
+                        st[q] = a;
+                        const unsigned long long t = sv[i];
+                        sv[i] = sv[q];
+                        sv[q] = t;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+        gv[i] = static_cast<uint32_t>(sv[i]);
+        gp[i] = static_cast<uint32_t>(sv[i] >> 32);
+    }
+    if (threadIdx.x == 0) *ng = n;
+}
+
 __global__ void ws_unpack_entries(const unsigned long long* __restrict__ val, size_t n,
                                   uint32_t* __restrict__ gv, uint32_t* __restrict__ gp) {
     PMA_GRID_STRIDE(i, n) {
@@ -661,21 +702,37 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
         auto* d_out = buf<unsigned long long>(ctx, "ws.coop_out", 2);
         unsigned long long* h_out = reinterpret_cast<unsigned long long*>(h_small + 8);
-        for (int64_t depth = static_cast<int64_t>(nb) - 1; depth >= 0; --depth) {
-            if (boff[depth + 1] == boff[depth]) continue;
-            PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + depth, 4, cudaMemcpyDeviceToHost, s));
-            PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
-            ctx->sync();
-            grow_records(h_small[4]);
-            const size_t n0 = h_small[0];
+        // depths that can hold entries, deepest first
+        std::vector<int64_t> depths;
+        for (int64_t depth = static_cast<int64_t>(nb) - 1; depth >= 0; --depth)
+            if (boff[depth + 1] != boff[depth]) depths.push_back(depth);
+        bool have_count = false;  // entry count of depths[di] read with the previous depth's sync
+        size_t n0 = 0;
+        for (size_t di = 0; di < depths.size(); ++di) {
+            const int64_t depth = depths[di];
+            if (!have_count) {
+                PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + depth, 4, cudaMemcpyDeviceToHost, s));
+                PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
+                ctx->sync();
+                grow_records(h_small[4]);
+                n0 = h_small[0];
+            }
+            have_count = false;
             if (n0 == 0) continue;
-            sort_pairs(ctx, ws.ent_time + boff[depth], srt_time, ws.ent_val + boff[depth], srt_val,
-                       static_cast<int64_t>(n0));
             int cur = 0;
-            ws_unpack_entries<<<grid_for(ctx, n0), 256, 0, s>>>(srt_val, n0, gvb[cur], gpb[cur]);
-            ctx->check_launch("ws_unpack_entries");
-            h_small[2] = static_cast<unsigned int>(n0);
-            PMA_CUDA(cudaMemcpyAsync(d_ng + cur, &h_small[2], 4, cudaMemcpyHostToDevice, s));
+            if (n0 <= static_cast<size_t>(kSmallBucket)) {
+                ws_sort_small<<<1, 1024, 0, s>>>(ws.ent_time + boff[depth], ws.ent_val + boff[depth],
+                                                 static_cast<unsigned>(n0), gvb[cur], gpb[cur], d_ng + cur);
+                ctx->check_launch("ws_sort_small");
+            } else {
+                sort_pairs(ctx, ws.ent_time + boff[depth], srt_time, ws.ent_val + boff[depth], srt_val,
+                           static_cast<int64_t>(n0));
+                ws_unpack_entries<<<grid_for(ctx, n0), 256, 0, s>>>(srt_val, n0, gvb[cur], gpb[cur]);
+                ctx->check_launch("ws_unpack_entries");
+                h_small[2] = static_cast<unsigned int>(n0);
+                PMA_CUDA(cudaMemcpyAsync(d_ng + cur, &h_small[2], 4, cudaMemcpyHostToDevice, s));
+            }
+            const int64_t next_depth = di + 1 < depths.size() ? depths[di + 1] : -1;
             KernelTimer kt(ctx, "ws_generations");
             while (true) {
                 const uint32_t dep = static_cast<uint32_t>(depth);
@@ -688,12 +745,19 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
                 PMA_CUDA(cudaMemcpyAsync(h_out, d_out, 16, cudaMemcpyDeviceToHost, s));
                 PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
                 PMA_CUDA(cudaMemcpyAsync(h_small + 6, d_ng, 8, cudaMemcpyDeviceToHost, s));
+                // the next depth's entries are final once this depth is done: read them along
+                if (next_depth >= 0)
+                    PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + next_depth, 4, cudaMemcpyDeviceToHost, s));
                 ctx->sync();
                 gen += h_out[0];
                 cur = static_cast<int>(h_out[1]);
                 grow_records(h_small[4]);
                 if (h_small[6 + cur] == 0) break;
                 PMA_REQUIRE(gen + kGensPerLaunch < kMaxGen, PMA_ERR_LIMIT, "pma_watershed: generation limit reached");
+            }
+            if (next_depth >= 0) {
+                n0 = h_small[0];
+                have_count = true;
             }
         }
         PMA_CUDA(cudaMemcpyAsync(&h_err, ws.err, 4, cudaMemcpyDeviceToHost, s));
