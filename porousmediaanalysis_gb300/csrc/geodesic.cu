@@ -123,83 +123,89 @@ __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
     }
 }
 
-// Processes bucket k: settle its voxels and relax their neighbours. One thread per
-// (entry, stencil position): the wavefront of a bucket is a thin shell of a few thousand to a
-// few hundred thousand voxels, and 27 threads per voxel keep enough loads in flight to hide
-// their latency; the neighbours of one voxel fall in one warp and share cache lines, and the
-// list is in voxel order, so neighbouring warps share them too. Each voxel is in the list
-// once, so a live entry (bucket(dist) == k) is settled exactly once, by its centre thread.
-template <class T>
-__global__ void geo_bucket(Geo g, int d3q7, T w1, T w2, T w3, T* __restrict__ dist,
-                           uint32_t* __restrict__ cavity, Frontier f, int k, uint32_t cavity_id) {
+// Processes bucket k: settle its voxels and relax their neighbours. One thread per list
+// entry: it reads its own distance, then issues the loads of all its neighbours' distances at
+// once (26 independent loads in flight per thread hide their latency; the list is in voxel
+// order, so a warp's loads of one stencil position fall on neighbouring addresses), then
+// lowers the neighbours it improves. Each voxel is in the list once, so a live entry
+// (bucket(dist) == k) is settled exactly once. Steps are in [1, 2), so pushes go to buckets
+// k + 1 and k + 2 only; they are counted per thread and added per warp at the end.
+template <class T, bool D3Q7>
+__global__ void __launch_bounds__(256) geo_bucket(Geo g, T w1, T w2, T w3, T* __restrict__ dist,
+                                                  uint32_t* __restrict__ cavity, Frontier f, int k,
+                                                  uint32_t cavity_id) {
     typedef typename Bits<T>::U U;
     const unsigned n = min(*f.list_n, f.cap);
     const uint32_t* list = f.list;
+    const long long sy = g.SY, sxy = static_cast<long long>(g.SX) * g.SY;
     unsigned long long my_settled = 0;
-    unsigned my_walls = 0;
-    const unsigned long long total = static_cast<unsigned long long>(n) * 27;
-    const unsigned lane = threadIdx.x & 31;
-    for (unsigned long long t = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; t < total;
-         t += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
-        const unsigned i = static_cast<unsigned>(t / 27);
-        const int j = static_cast<int>(t - static_cast<unsigned long long>(i) * 27);
+    unsigned my_walls = 0, c1 = 0, c2 = 0;
+    uint32_t* bm1 = f.bits + static_cast<size_t>((k + 1) & 3) * f.nwords;
+    uint32_t* bm2 = f.bits + static_cast<size_t>((k + 2) & 3) * f.nwords;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t v = list[i];
         const T dv = dist[v];
-        bool push = false;
-        int pb = 0;
-        size_t w = 0;
-        if (Bits<T>::bucket(dv) == k) {  // else a stale entry: the voxel moved to a lower bucket
-            const int y = static_cast<int>(v % g.SY);
-            const uint32_t zx = v / g.SY;
-            const int x = static_cast<int>(zx % g.SX);
-            const int z = static_cast<int>(zx / g.SX);
-            if (j == 13) {  // centre: settle
-                cavity[v] = cavity_id;
-                ++my_settled;
-                if (x == 0) my_walls |= 1u;
-                if (x == g.SX - 1 && g.SX > 1) my_walls |= 2u;
-                if (y == 0) my_walls |= 4u;
-                if (y == g.SY - 1 && g.SY > 1) my_walls |= 8u;
-                if (z == 0) my_walls |= 16u;
-                if (z == g.SZ - 1 && g.SZ > 1) my_walls |= 32u;
-            } else {
-                const int dx = j / 9 - 1, dy = (j / 3) % 3 - 1, dz = j % 3 - 1;
-                const int kk = dx * dx + dy * dy + dz * dz;
-                const int nx = x + dx, ny = y + dy, nz = z + dz;
-                if ((!d3q7 || kk == 1) && nx >= 0 && nx < g.SX && ny >= 0 && ny < g.SY && nz >= 0 &&
-                    nz < g.SZ) {
-                    w = g.idx(nx, ny, nz);
-                    // solid voxels hold -1 and never take the (positive) new distance, so the
-                    // distance alone decides; no separate read of the solid mask
-                    const T step = d3q7 ? static_cast<T>(1) : (kk == 1 ? w1 : (kk == 2 ? w2 : w3));
-                    const T nd = Bits<T>::add(dv, step);
-                    if (nd < dist[w]) {
-                        const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
-                        if (Bits<T>::to(nd) < old) {
-                            pb = Bits<T>::bucket(nd);
-                            const uint32_t bit = 1u << (w & 31);
-                            push = !(atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit) & bit);
-                        }
+        if (Bits<T>::bucket(dv) != k) continue;  // stale: the voxel moved to a lower bucket
+        const int y = static_cast<int>(v % g.SY);
+        const uint32_t zx = v / g.SY;
+        const int x = static_cast<int>(zx % g.SX);
+        const int z = static_cast<int>(zx / g.SX);
+        cavity[v] = cavity_id;
+        ++my_settled;
+        const bool xl = x > 0, xh = x < g.SX - 1, yl = y > 0, yh = y < g.SY - 1, zl = z > 0, zh = z < g.SZ - 1;
+        if (!xl) my_walls |= 1u;
+        if (!xh && g.SX > 1) my_walls |= 2u;
+        if (!yl) my_walls |= 4u;
+        if (!yh && g.SY > 1) my_walls |= 8u;
+        if (!zl) my_walls |= 16u;
+        if (!zh && g.SZ > 1) my_walls |= 32u;
+        const T nd1 = Bits<T>::add(dv, D3Q7 ? static_cast<T>(1) : w1);
+        const T nd2 = Bits<T>::add(dv, w2), nd3 = Bits<T>::add(dv, w3);
+        T nb[27];
+#pragma unroll
+        for (int j = 0; j < 27; ++j) {
+            const int dx = j / 9 - 1, dy = (j / 3) % 3 - 1, dz = j % 3 - 1;
+            const int kk = dx * dx + dy * dy + dz * dz;
+            if (kk == 0 || (D3Q7 && kk != 1)) continue;
+            const bool ok = (dx < 0 ? xl : (dx > 0 ? xh : true)) && (dy < 0 ? yl : (dy > 0 ? yh : true)) &&
+                            (dz < 0 ? zl : (dz > 0 ? zh : true));
+            // out of the box reads as -1, like a solid voxel: never improved
+            nb[j] = ok ? dist[static_cast<long long>(v) + dz * sxy + dx * sy + dy] : static_cast<T>(-1);
+        }
+#pragma unroll
+        for (int j = 0; j < 27; ++j) {
+            const int dx = j / 9 - 1, dy = (j / 3) % 3 - 1, dz = j % 3 - 1;
+            const int kk = dx * dx + dy * dy + dz * dz;
+            if (kk == 0 || (D3Q7 && kk != 1)) continue;
+            const T nd = kk == 1 ? nd1 : (kk == 2 ? nd2 : nd3);
+            if (nd < nb[j]) {
+                const size_t w = static_cast<size_t>(static_cast<long long>(v) + dz * sxy + dx * sy + dy);
+                const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
+                if (Bits<T>::to(nd) < old) {
+                    const int pb = Bits<T>::bucket(nd);
+                    const uint32_t bit = 1u << (w & 31);
+                    if (pb == k + 1) {
+                        c1 += (atomicOr(&bm1[w >> 5], bit) & bit) ? 0u : 1u;
+                    } else if (pb == k + 2) {
+                        c2 += (atomicOr(&bm2[w >> 5], bit) & bit) ? 0u : 1u;
+                    } else if (!(atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit) & bit)) {
+                        atomicAdd(&f.count[pb & 3], 1u);  // not reachable with steps in [1, 2)
                     }
                 }
             }
         }
-        // newly set bits, counted per warp and target bitmap (buckets k + 1 and k + 2 only:
-        // steps are in [1, 2))
-        const unsigned active = __activemask();
-        for (int tb = 1; tb <= 2; ++tb) {
-            const unsigned m = __ballot_sync(active, push && pb == k + tb);
-            if (m && static_cast<int>(lane) == __ffs(m) - 1) atomicAdd(&f.count[(k + tb) & 3], static_cast<unsigned>(__popc(m)));
-        }
-        if (push && (pb < k + 1 || pb > k + 2)) atomicAdd(&f.count[pb & 3], 1u);  // not reachable
     }
     for (int o = 16; o > 0; o >>= 1) {
         my_settled += __shfl_xor_sync(0xFFFFFFFFu, my_settled, o);
         my_walls |= __shfl_xor_sync(0xFFFFFFFFu, my_walls, o);
+        c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, o);
+        c2 += __shfl_xor_sync(0xFFFFFFFFu, c2, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (my_settled) atomicAdd(f.settled, my_settled);
         if (my_walls) atomicOr(f.walls, my_walls);
+        if (c1) atomicAdd(&f.count[(k + 1) & 3], c1);
+        if (c2) atomicAdd(&f.count[(k + 2) & 3], c2);
     }
 }
 
@@ -365,7 +371,8 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
             for (int i = 0; i < max_buckets_per_sync; ++i, ++k) {
                 geo_next<<<1, 1, 0, s>>>(f, k);
                 geo_compact<<<compact_grid, 256, 0, s>>>(f, k);
-                geo_bucket<T><<<bucket_grid, 256, 0, s>>>(g, d3q7, w1, w2, w3, dist, cavity, f, k, cavity_id);
+                if (d3q7) geo_bucket<T, true><<<bucket_grid, 256, 0, s>>>(g, w1, w2, w3, dist, cavity, f, k, cavity_id);
+                else geo_bucket<T, false><<<bucket_grid, 256, 0, s>>>(g, w1, w2, w3, dist, cavity, f, k, cavity_id);
             }
             ctx->count_launch(3 * max_buckets_per_sync - 1);
             ctx->check_launch("geo_bucket");
