@@ -64,6 +64,7 @@ struct WsState {
     unsigned int* err;
     uint32_t* slot_gen;           // generation stamp of same-depth claims, per event slot
     uint32_t* slot_voxel;
+    uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
     unsigned int* bfill;
     unsigned long long* ent_time;
@@ -162,60 +163,77 @@ __device__ __noinline__ void ws_extend(uint32_t* ext, unsigned int* ext_count, u
 // Touch events of the generation's nodes. Phase 0 claims: the smallest touch time of each
 // unclaimed voxel wins. Claim keys carry a generation tag that decreases from one generation
 // to the next, so a key left by an earlier generation is larger than any key of the current
-// one and ckey never needs clearing. Phase 1 resolves: the winner records its claim, and
-// every other touch by a pore other than the voxel's owner - the winner's pore for a voxel
-// claimed in this generation, else the stored claim - is an extension.
+// one and ckey never needs clearing. A touch of a voxel claimed in an earlier generation is
+// final in phase 0 already: it is an extension when the toucher is not the owner (claims
+// never change, and extensions keep each pore's smallest time, so the order of recording
+// does not matter). Phase 0 flags, per event, a touch of an unclaimed voxel; phase 1 resolves
+// only those: the winner records its claim, and every other touch by a pore other than the
+// winner's is an extension.
 // One thread per event (node i, stencil position j): seq = i * 27 + j.
 // All generations of a launch run in one kernel (see ws_generations), so data written by
 // other blocks earlier in the launch is read with __ldcg (L2, not a possibly stale L1 line);
 // only the radii, which never change, go through the read-only path.
-// ws_touch_event returns true when phase 1 stamps a same-depth claim (a node of the next
-// generation).
-template <int kPhase>
-__device__ __forceinline__ bool ws_touch_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
+__device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
                                                unsigned long long seq, uint32_t depth, unsigned long long gen,
                                                unsigned long long tag) {
     const unsigned long long i = seq / 27;
     const int j = static_cast<int>(seq - i * 27);
+    uint8_t touched = 0;
     int dx, dy, dz;
-    if (!stencil_offset(j, s.d3q7, dx, dy, dz)) return false;
+    if (stencil_offset(j, s.d3q7, dx, dy, dz)) {
+        const uint32_t v = __ldcg(gv + i);
+        const uint32_t pore = __ldcg(gp + i);
+        int x, y, z;
+        s.g.coords(v, x, y, z);
+        const int nx = x + dx, ny = y + dy, nz = z + dz;
+        if (!s.g.inside(nx, ny, nz)) {  // WC.cpp:140-144
+            s.pbound[pore] = 1;
+        } else {
+            const size_t w = s.g.idx(nx, ny, nz);
+            const uint32_t r = __ldg(s.crad + w);
+            if (r != 0 && r <= depth) {  // WC.cpp:152-156
+                const uint32_t c = __ldcg(s.claim + w);
+                if (c == 0) {
+                    atomicMin(&s.ckey[w], (tag << 40) | seq);
+                    touched = 1;
+                } else if (c - 1 != pore) {
+                    ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
+                }
+            }
+        }
+    }
+    s.ev_touch[seq] = touched;
+}
+
+// Returns true when the event stamps a same-depth claim (a node of the next generation).
+__device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
+                                                 unsigned long long seq, uint32_t depth, unsigned long long gen) {
+    if (!__ldcg(s.ev_touch + seq)) return false;
+    const unsigned long long i = seq / 27;
+    const int j = static_cast<int>(seq - i * 27);
+    int dx, dy, dz;
+    stencil_offset(j, s.d3q7, dx, dy, dz);
     const uint32_t v = __ldcg(gv + i);
     const uint32_t pore = __ldcg(gp + i);
-    int x, y, z;
-    s.g.coords(v, x, y, z);
-    const int nx = x + dx, ny = y + dy, nz = z + dz;
-    if (!s.g.inside(nx, ny, nz)) {  // WC.cpp:140-144
-        if (kPhase == 0) s.pbound[pore] = 1;
-        return false;
-    }
-    const size_t w = s.g.idx(nx, ny, nz);
-    const uint32_t r = __ldg(s.crad + w);
-    if (r == 0 || r > depth) return false;  // WC.cpp:152-156
-    if (kPhase == 0) {
-        if (__ldcg(s.claim + w) == 0) atomicMin(&s.ckey[w], (tag << 40) | seq);
-        return false;
-    }
-    const unsigned long long k = __ldcg(s.ckey + w);
-    uint32_t owner;
-    if ((k >> 40) == tag) {  // unclaimed when this generation started
-        const unsigned long long wseq = k & kSeqMask;
-        if (wseq == seq) {
-            s.claim[w] = pore + 1;
-            if (r == depth) {
-                s.slot_voxel[seq] = static_cast<uint32_t>(w);
-                s.slot_gen[seq] = static_cast<uint32_t>(gen);
-                return true;
-            }
-            const unsigned pos = atomicAdd(&s.bfill[r], 1u);
-            const unsigned long long at = s.boff[r] + pos;
-            s.ent_time[at] = (gen << 40) | seq;
-            s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
-            return false;
+    // the neighbour is inside the box (phase 0 touched it)
+    const size_t w = static_cast<size_t>(static_cast<long long>(v) +
+                                         (static_cast<long long>(dz) * s.g.SX + dx) * s.g.SY + dy);
+    const unsigned long long wseq = __ldcg(s.ckey + w) & kSeqMask;
+    if (wseq == seq) {
+        s.claim[w] = pore + 1;
+        const uint32_t r = __ldg(s.crad + w);
+        if (r == depth) {
+            s.slot_voxel[seq] = static_cast<uint32_t>(w);
+            s.slot_gen[seq] = static_cast<uint32_t>(gen);
+            return true;
         }
-        owner = __ldcg(gp + wseq / 27);
-    } else {
-        owner = __ldcg(s.claim + w) - 1;
+        const unsigned pos = atomicAdd(&s.bfill[r], 1u);
+        const unsigned long long at = s.boff[r] + pos;
+        s.ent_time[at] = (gen << 40) | seq;
+        s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
+        return false;
     }
+    const uint32_t owner = __ldcg(gp + wseq / 27);
     if (owner != pore)
         ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
     return false;
@@ -325,7 +343,7 @@ __global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t
         uint32_t* nv = cur ? gv0 : gv1;
         uint32_t* np_ = cur ? gp0 : gp1;
         const unsigned long long tag = kMaxGen - gen;
-        for (unsigned long long seq = tid; seq < nev; seq += stride) ws_touch_event<0>(s, gv, gp, seq, depth, gen, tag);
+        for (unsigned long long seq = tid; seq < nev; seq += stride) ws_claim_event(s, gv, gp, seq, depth, gen, tag);
         grid.sync();
         // Phase 1 by chunks of kChunk events (4 per thread), so that each block also counts
         // its chunk's same-depth claims for the compaction.
@@ -334,7 +352,7 @@ __global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t
             unsigned int local = 0;
             for (int k = 0; k < 4; ++k) {
                 const unsigned long long seq = c * kChunk + k * (kChunk / 4) + threadIdx.x;
-                if (seq < nev && ws_touch_event<1>(s, gv, gp, seq, depth, gen, tag)) ++local;
+                if (seq < nev && ws_resolve_event(s, gv, gp, seq, depth, gen)) ++local;
             }
             for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
             if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = local;
@@ -661,6 +679,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         const size_t max_events = max_bucket * 27;
         ws.slot_gen = buf<uint32_t>(ctx, "ws.slot_gen", max_events);
         ws.slot_voxel = buf<uint32_t>(ctx, "ws.slot_voxel", max_events);
+        ws.ev_touch = buf<uint8_t>(ctx, "ws.ev_touch", max_events);  // written for every event by phase 0
         PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));  // generations start at 1
         unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", (max_events + kChunk - 1) / kChunk);
         PMA_CUDA(cudaMemcpyAsync(d_boff, boff.data(), (nb + 1) * 8ull, cudaMemcpyHostToDevice, s));
