@@ -36,6 +36,8 @@ WORKLOADS = {
                    desc="320^3 thresholded Gaussian random field, sigma 3, porosity 0.65 (profiling size)"),
     "spinodal1024": dict(kind="spinodal", shape=(1024, 1024, 1024), seed=3,
                          desc="1024^3 leveled-wave spinodal, 1000 waves, wavelength 48, porosity 0.70"),
+    "spinodal384": dict(kind="spinodal", shape=(384, 384, 384), seed=3,
+                        desc="384^3 leveled-wave spinodal, 1000 waves, wavelength 48, porosity 0.70 (profiling size)"),
     "union128": dict(kind="union", shape=(128, 128, 128), seed=1,
                      desc="128^3 union of 300 spheres, radii U[5,10]"),
 }

@@ -17,11 +17,12 @@
 //
 // Gather: the volume is cut into 8^3 tiles; every kept centre is listed in each tile its
 // ball reaches, unless its key is below the tile's floor (the largest key of a ball covering
-// the whole tile, which every voxel of the tile is covered by). One CTA per tile sorts its
-// list by key in shared memory (descending), and each voxel takes the first entry whose ball
-// covers it: that entry is the covering centre of largest key, i.e. the reference's winner.
-// A voxel stops at its winner, so the work is the winner's rank in the tile list rather than
-// the ball volumes a scatter would touch.
+// the whole tile, which every voxel of the tile is covered by). One CTA per tile orders its
+// list by radius in shared memory, and each warp of voxels takes, per voxel, the largest key
+// among the entries whose ball covers it: the reference's winner. A warp only tests entries
+// that reach its 1 x 4 x 8 box and beat its lanes' smallest key so far, and stops where the
+// radius order shows that no later entry can, so the work is close to the winners' ranks in
+// the list rather than the ball volumes a scatter would touch.
 #include <thrust/iterator/counting_iterator.h>
 
 #include <vector>
@@ -34,7 +35,7 @@ namespace {
 constexpr uint32_t kExactTable = 1u << 16;
 constexpr int kTile = 8;          // tile edge
 constexpr int kTileVox = 512;     // voxels (and threads) per tile
-constexpr int kListCap = 2048;    // entries sorted in shared memory; longer lists go in chunks
+constexpr int kListCap = 2048;    // entries ordered in shared memory at a time; longer lists go in chunks
 
 __device__ __forceinline__ uint32_t isqrt_u32(uint32_t n) {
     uint32_t r = static_cast<uint32_t>(sqrtf(static_cast<float>(n)));
@@ -255,76 +256,162 @@ __device__ __forceinline__ bool covers(int4 c, int vx, int vy, int vz) {
     return d2 <= static_cast<uint32_t>(c.w);
 }
 
+__device__ __forceinline__ unsigned long long pos_key(int4 c, Grid g) {
+    const uint32_t lex = (static_cast<uint32_t>(c.x) * g.SY + static_cast<uint32_t>(c.y)) * static_cast<uint32_t>(g.SZ) +
+                         static_cast<uint32_t>(c.z);
+    return (static_cast<unsigned long long>(static_cast<uint32_t>(c.w)) << 32) | (0xFFFFFFFFu - lex);
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = t < v ? t : v;
+    }
+    return v;
+}
+
 // One CTA per tile of the z-range starting at tz0: winner key of each voxel.
+//
+// The tile's list is taken in chunks of up to kListCap entries. Each chunk is decoded into
+// shared memory ordered by radius, largest first (a counting sort on r^2 when the chunk's r^2
+// span fits kSortBins, else left in list order). A warp covers a 1 x 4 x 8 box of voxels and
+// keeps, per lane, the largest covering key so far (best). It reads the chunk 32 entries at a
+// time: an entry can matter only if its ball reaches the warp's box and its key exceeds the
+// smallest best of the warp's lanes; the lanes test every such entry against their own voxel.
+// In a chunk sorted by radius the warp stops once the next entry's r^2 is below the smallest
+// best's r^2 (every later entry's key is smaller). The result is the largest covering key over
+// the whole list, i.e. the covering centre of largest key.
+constexpr int kSortBins = 2048;
+
 __global__ void __launch_bounds__(kTileVox) balls_tile_gather(
     const uint32_t* __restrict__ edt2, Grid g, Tiles t, int tz0,
     const unsigned int* __restrict__ tcount, const unsigned long long* __restrict__ toff,
     unsigned long long base, const unsigned long long* __restrict__ entries,
     unsigned long long* __restrict__ keys, unsigned int* __restrict__ err) {
-    __shared__ unsigned long long s_key[kListCap];
     __shared__ int4 s_pos[kListCap];
+    __shared__ unsigned int s_bin[kSortBins];
+    __shared__ unsigned int s_rmin, s_rmax, s_wsum[kTileVox / 32];
     const size_t tile = static_cast<size_t>(tz0) * t.TX * t.TY + blockIdx.x;
     const int ty = static_cast<int>(tile % t.TY);
     const size_t rest = tile / t.TY;
     const int tx = static_cast<int>(rest % t.TX);
     const int tz = static_cast<int>(rest / t.TX);
-    // voxel of this thread: y fastest, then x, then z (a warp covers a 4 x 8 patch)
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // voxel of this thread: y fastest, then x, then z (a warp covers a 1 x 4 x 8 box)
     const int vy = ty * kTile + (threadIdx.x & 7);
     const int vx = tx * kTile + ((threadIdx.x >> 3) & 7);
     const int vz = tz * kTile + (threadIdx.x >> 6);
     const bool inside = vx < g.SX && vy < g.SY && vz < g.SZ;
     const size_t v = inside ? g.idx(vx, vy, vz) : 0;
     const bool void_voxel = inside && edt2[v] != 0;
+    // the warp's box
+    const int bx0 = tx * kTile + (warp & 1) * 4, by0 = ty * kTile, bz = vz;
     const unsigned int L = tcount[tile];
     const unsigned long long* list = entries + (toff[tile] - base);
-    unsigned long long best = 0;
-    if (L <= static_cast<unsigned int>(kListCap)) {
-        unsigned int N = 1;
-        while (N < L) N <<= 1;
-        for (unsigned int i = threadIdx.x; i < N; i += blockDim.x) s_key[i] = (i < L) ? list[i] : 0ull;
+    unsigned long long best = void_voxel ? 0ull : ~0ull;
+    for (unsigned int c0 = 0; c0 < L; c0 += kListCap) {
+        const unsigned int m = min(static_cast<unsigned int>(kListCap), L - c0);
+        // radius span of the chunk; up to four entries per thread stay in registers
+        constexpr int kPer = kListCap / kTileVox;
+        unsigned long long k[kPer];
+        if (threadIdx.x == 0) {
+            s_rmin = 0xFFFFFFFFu;
+            s_rmax = 0;
+        }
+        for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) s_bin[i] = 0;
         __syncthreads();
-        // bitonic sort, descending
-        for (unsigned int k = 2; k <= N; k <<= 1) {
-            for (unsigned int j = k >> 1; j > 0; j >>= 1) {
-                for (unsigned int i = threadIdx.x; i < N; i += blockDim.x) {
-                    const unsigned int p = i ^ j;
-                    if (p > i) {
-                        const unsigned long long a = s_key[i], b = s_key[p];
-                        const bool desc = (i & k) == 0;
-                        if (desc ? (a < b) : (a > b)) {
-                            s_key[i] = b;
-                            s_key[p] = a;
-                        }
-                    }
-                }
-                __syncthreads();
+        unsigned int rmin = 0xFFFFFFFFu, rmax = 0;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const unsigned int i = threadIdx.x + q * kTileVox;
+            k[q] = i < m ? list[c0 + i] : 0ull;
+            if (i < m) {
+                rmin = min(rmin, static_cast<unsigned int>(k[q] >> 32));
+                rmax = max(rmax, static_cast<unsigned int>(k[q] >> 32));
             }
         }
-        for (unsigned int i = threadIdx.x; i < L; i += blockDim.x) s_pos[i] = decode_key(s_key[i], g);
-        __syncthreads();
-        if (void_voxel) {
-            for (unsigned int i = 0; i < L; ++i) {
-                if (covers(s_pos[i], vx, vy, vz)) {
-                    best = s_key[i];
-                    break;
-                }
-            }
+        rmin = __reduce_min_sync(0xFFFFFFFFu, rmin);
+        rmax = __reduce_max_sync(0xFFFFFFFFu, rmax);
+        if (lane == 0) {
+            atomicMin(&s_rmin, rmin);
+            atomicMax(&s_rmax, rmax);
         }
-    } else {
-        // long list: unsorted chunks, keep the largest covering key
-        for (unsigned int c0 = 0; c0 < L; c0 += kListCap) {
-            const unsigned int m = min(static_cast<unsigned int>(kListCap), L - c0);
-            __syncthreads();
-            for (unsigned int i = threadIdx.x; i < m; i += blockDim.x) {
-                s_key[i] = list[c0 + i];
-                s_pos[i] = decode_key(s_key[i], g);
+        __syncthreads();
+        const unsigned int r_hi = s_rmax;
+        const bool sorted = r_hi - s_rmin < static_cast<unsigned int>(kSortBins);
+        unsigned int rank[kPer];
+        if (sorted) {  // counting sort, descending r^2: bin = r_hi - r^2
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const unsigned int i = threadIdx.x + q * kTileVox;
+                rank[q] = i < m ? atomicAdd(&s_bin[r_hi - static_cast<unsigned int>(k[q] >> 32)], 1u) : 0u;
             }
             __syncthreads();
-            if (void_voxel) {
-                for (unsigned int i = 0; i < m; ++i)
-                    if (s_key[i] > best && covers(s_pos[i], vx, vy, vz)) best = s_key[i];
+            // exclusive scan of the bins, four per thread
+            unsigned int b4[kSortBins / kTileVox], sum = 0;
+#pragma unroll
+            for (int q = 0; q < kSortBins / kTileVox; ++q) {
+                b4[q] = s_bin[threadIdx.x * (kSortBins / kTileVox) + q];
+                sum += b4[q];
+            }
+            unsigned int incl = sum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int t2 = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= static_cast<unsigned>(o)) incl += t2;
+            }
+            if (lane == 31) s_wsum[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                unsigned int w = lane < kTileVox / 32 ? s_wsum[lane] : 0u;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned int t2 = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                    if (lane >= static_cast<unsigned>(o)) w += t2;
+                }
+                if (lane < kTileVox / 32) s_wsum[lane] = w;
+            }
+            __syncthreads();
+            unsigned int run = (warp ? s_wsum[warp - 1] : 0u) + incl - sum;
+#pragma unroll
+            for (int q = 0; q < kSortBins / kTileVox; ++q) {
+                s_bin[threadIdx.x * (kSortBins / kTileVox) + q] = run;
+                run += b4[q];
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const unsigned int i = threadIdx.x + q * kTileVox;
+            if (i < m) {
+                const unsigned int at = sorted ? s_bin[r_hi - static_cast<unsigned int>(k[q] >> 32)] + rank[q] : i;
+                s_pos[at] = decode_key(k[q], g);
             }
         }
+        __syncthreads();
+        // the warp's pass over the chunk
+        for (unsigned int e0 = 0; e0 < m; e0 += 32) {
+            const unsigned long long mb = warp_min_u64(best);
+            if (mb == ~0ull) break;  // no void voxel left to improve
+            if (sorted && static_cast<uint32_t>(s_pos[e0].w) < static_cast<uint32_t>(mb >> 32)) break;
+            bool cand = false;
+            if (e0 + lane < m) {
+                const int4 c = s_pos[e0 + lane];
+                if (pos_key(c, g) > mb) {  // can beat some lane; does the ball reach the box?
+                    const int dx = c.x < bx0 ? bx0 - c.x : (c.x > bx0 + 3 ? c.x - bx0 - 3 : 0);
+                    const int dy = c.y < by0 ? by0 - c.y : (c.y > by0 + 7 ? c.y - by0 - 7 : 0);
+                    const int dz = c.z < bz ? bz - c.z : (c.z > bz ? c.z - bz : 0);
+                    cand = covers(make_int4(dx, dy, dz, c.w), 0, 0, 0);
+                }
+            }
+            unsigned int mask = __ballot_sync(0xFFFFFFFFu, cand);
+            while (mask) {
+                const int b = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int4 c = s_pos[e0 + b];
+                const unsigned long long kc = pos_key(c, g);
+                if (kc > best && void_voxel && covers(c, vx, vy, vz)) best = kc;
+            }
+        }
+        __syncthreads();
     }
     if (inside) {
         if (void_voxel && best == 0) atomicOr(err, 2u);  // no kept ball covers a void voxel

@@ -144,3 +144,37 @@ def test_containing_balls_properties_512(ctx):
     assert int((mask == 255).sum()) == nb
     crad2b, cxb, _, _, maskb, nbb = pma.set_containing_balls(ctx, edt2, mx)
     assert bool((crad2b == crad2).all()) and bool((cxb == cx).all()) and nbb == nb
+
+
+def _balls_vs_oracle(ctx, oracle_mod, vol):
+    import torch
+    import porousmediaanalysis_gb300 as pma
+    solid = torch.from_numpy(np.ascontiguousarray(vol, dtype=np.uint8)).cuda()
+    edt2, mx, _ = pma.compute_euclidean_distances(ctx, solid)
+    crad2, cx, cy, cz, mask, nb = pma.set_containing_balls(ctx, edt2, mx)
+    e, omx, _ = oracle_mod.edt(vol)
+    assert mx == omx
+    ocrad, ocx, ocy, ocz = oracle_mod.containing_balls(e, omx)
+    u32 = lambda t: t.cpu().numpy().view(np.uint32)
+    assert (u32(crad2) == ocrad).all()
+    assert (u32(cx) == ocx).all() and (u32(cy) == ocy).all() and (u32(cz) == ocz).all()
+    omask, onb = oracle_mod.max_ball_mask(ocx, ocy, ocz)
+    assert (mask.cpu().numpy() == omask).all() and nb == onb
+
+
+def test_containing_balls_long_tile_lists(ctx, oracle_mod):
+    """96^3 leveled-wave spinodal (wavelength 48): radii up to sqrt(533), tile lists of up to
+    several thousand centres, so the gather takes them in several shared-memory chunks."""
+    from porousmediaanalysis_gb300 import synth
+    vol = synth.spinodal((96, 96, 96), device="cpu").numpy()
+    _balls_vs_oracle(ctx, oracle_mod, vol)
+
+
+def test_containing_balls_wide_radius_span(ctx, oracle_mod):
+    """A 44^3 box with two solid voxels: tile lists of up to 40 000 centres (twenty chunks),
+    and in two tiles squared radii spanning more than the gather's counting sort (2048), so
+    those chunks are scanned in fill order."""
+    vol = np.zeros((44, 44, 44), np.uint8)
+    vol[0, 0, 0] = 1
+    vol[27, 11, 38] = 1
+    _balls_vs_oracle(ctx, oracle_mod, vol)
