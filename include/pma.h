@@ -65,7 +65,8 @@ uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
  * pass a buffer large enough for the whole report. Returns its full length. */
 int pma_ctx_set_timing(pma_ctx* ctx, int enable);
 size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap);
-/* Device bytes held by ctx's scratch cache; pma_ctx_trim releases them. */
+/* Device bytes held by ctx's scratch cache and its memory pool (freed blocks are kept for
+   reuse), batch lanes included; pma_ctx_trim releases them. */
 size_t pma_ctx_scratch_bytes(const pma_ctx* ctx);
 int pma_ctx_trim(pma_ctx* ctx);
 

@@ -283,7 +283,7 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
 // the whole list, i.e. the covering centre of largest key.
 constexpr int kSortBins = 2048;
 
-__global__ void __launch_bounds__(kTileVox) balls_tile_gather(
+__global__ void __launch_bounds__(kTileVox, 3) balls_tile_gather(
     const uint32_t* __restrict__ edt2, Grid g, Tiles t, int tz0,
     const unsigned int* __restrict__ tcount, const unsigned long long* __restrict__ toff,
     unsigned long long base, const unsigned long long* __restrict__ entries,
@@ -341,10 +341,17 @@ __global__ void __launch_bounds__(kTileVox) balls_tile_gather(
         const bool sorted = r_hi - s_rmin < static_cast<unsigned int>(kSortBins);
         unsigned int rank[kPer];
         if (sorted) {  // counting sort, descending r^2: bin = r_hi - r^2
+            // equal radii are common: lanes with the same bin take their ranks with one atomic
 #pragma unroll
             for (int q = 0; q < kPer; ++q) {
                 const unsigned int i = threadIdx.x + q * kTileVox;
-                rank[q] = i < m ? atomicAdd(&s_bin[r_hi - static_cast<unsigned int>(k[q] >> 32)], 1u) : 0u;
+                const unsigned int bin = i < m ? r_hi - static_cast<unsigned int>(k[q] >> 32) : 0xFFFFFFFFu;
+                const unsigned int peers = __match_any_sync(0xFFFFFFFFu, bin);
+                const int leader = __ffs(peers) - 1;
+                unsigned int at = 0;
+                if (bin != 0xFFFFFFFFu && static_cast<int>(lane) == leader) at = atomicAdd(&s_bin[bin], __popc(peers));
+                at = __shfl_sync(0xFFFFFFFFu, at, leader);
+                rank[q] = at + __popc(peers & ((1u << lane) - 1u));
             }
             __syncthreads();
             // exclusive scan of the bins, four per thread
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(kTileVox) balls_tile_gather(
                 if (kc > best && void_voxel && covers(c, vx, vy, vz)) best = kc;
             }
         }
-        __syncthreads();
+        if (c0 + kListCap < L) __syncthreads();  // before the next chunk replaces s_pos
     }
     if (inside) {
         if (void_voxel && best == 0) atomicOr(err, 2u);  // no kept ball covers a void voxel

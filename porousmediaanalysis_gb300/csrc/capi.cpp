@@ -27,7 +27,10 @@ static cudaMemPool_t ensure_pool(pma_ctx* c) {
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = c->device;
     PMA_CUDA(cudaMemPoolCreate(&c->pool, &props));
-    unsigned long long keep = 256ull << 20;  // freed blocks kept for reuse beyond this go back
+    // Freed blocks stay in the pool for reuse until pma_ctx_trim: buffers that grow inside a
+    // call (e.g. the watershed's shared-voxel records) would otherwise go back to the driver
+    // at every synchronisation and be mapped afresh, gigabytes at a time, on the next call.
+    unsigned long long keep = ~0ull;
     PMA_CUDA(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
     return c->pool;
 }
@@ -56,6 +59,12 @@ void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
     }
     b.bytes = want;
     return b.ptr;
+}
+
+cudaStream_t pma_ctx::side_stream() {
+    if (!copy_stream) PMA_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    if (!copy_event) PMA_CUDA(cudaEventCreateWithFlags(&copy_event, cudaEventDisableTiming));
+    return copy_stream;
 }
 
 void pma_ctx::release(const std::string& tag) {
@@ -149,6 +158,11 @@ int pma_ctx_destroy(pma_ctx* ctx) {
         cudaStreamSynchronize(ctx->stream);
         if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
         if (ctx->sync_event) cudaEventDestroy(ctx->sync_event);
+        if (ctx->copy_stream) {
+            cudaStreamSynchronize(ctx->copy_stream);
+            cudaStreamDestroy(ctx->copy_stream);
+        }
+        if (ctx->copy_event) cudaEventDestroy(ctx->copy_event);
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
         if (ctx->count_word) cudaFreeHost(ctx->count_word);
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -227,6 +241,10 @@ size_t pma_ctx_scratch_bytes(const pma_ctx* ctx) {
     size_t s = 0;
     if (ctx) {
         for (auto& kv : ctx->cache) s += kv.second.bytes;
+        // the pool also holds freed blocks kept for reuse
+        unsigned long long reserved = 0;
+        if (ctx->pool && cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess)
+            s = std::max<size_t>(s, static_cast<size_t>(reserved));
         for (const pma_ctx* lane : ctx->lanes) s += pma_ctx_scratch_bytes(lane);
     }
     return s;

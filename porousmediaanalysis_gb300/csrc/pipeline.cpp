@@ -53,9 +53,18 @@ Fields alloc_fields(pma_ctx* ctx, size_t n, bool pores, bool geo, bool geo64) {
 }
 
 template <class T>
-void d2h(pma_ctx* ctx, T* host, const T* dev, size_t n) {
-    if (host && dev) PMA_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+void d2h(cudaStream_t s, T* host, const T* dev, size_t n) {
+    if (host && dev) PMA_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, s));
 }
+
+// Waits for the context's side stream on every exit, so that no copy into the caller's
+// buffers is left running when the call returns (an error included).
+struct SideJoin {
+    pma_ctx* ctx = nullptr;
+    ~SideJoin() {
+        if (ctx) cudaStreamSynchronize(ctx->copy_stream);
+    }
+};
 
 }  // namespace
 }  // namespace pma
@@ -63,8 +72,7 @@ void d2h(pma_ctx* ctx, T* host, const T* dev, size_t n) {
 namespace pma {
 
 // The chain on device fields of one volume (f.solid filled); tables and statistics go to out.
-static void run_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const pma_options& o, pma_outputs* out) {
-    const bool geo64 = o.run_geodesic && o.geodesic_fp64;
+static void run_pore_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const pma_options& o, pma_outputs* out) {
     out->pores = nullptr;
     out->watershed = nullptr;
     out->n_cavities = 0;
@@ -77,6 +85,10 @@ static void run_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const pma_op
         out->watershed = watershed(ctx, out->pores, f.crad2, dims, o.stencil, out->edt_stats.max_edt2,
                                    f.labels_ws);
     }
+}
+
+static void run_geo_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const pma_options& o, pma_outputs* out) {
+    const bool geo64 = o.run_geodesic && o.geodesic_fp64;
     if (o.run_geodesic && !geo64)
         out->n_cavities = geodesic<float>(ctx, f.solid, dims, o.stencil, f.dist32, f.cavity, out->cavities, 16);
     else if (o.run_geodesic)
@@ -98,21 +110,38 @@ void run_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims, cons
     Fields f = alloc_fields(ctx, n, o.run_pores != 0, o.run_geodesic != 0 && !geo64, geo64);
     if (geo64) f.cavity = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
     PMA_CUDA(cudaMemcpyAsync(f.solid, h_solid, n, cudaMemcpyHostToDevice, ctx->stream));
-    run_chain(ctx, f, dims, o, out);
-    if (o.run_pores) {
-        d2h(ctx, out->edt2, f.edt2, n);
-        d2h(ctx, out->crad2, f.crad2, n);
-        d2h(ctx, out->cx, f.cx, n);
-        d2h(ctx, out->cy, f.cy, n);
-        d2h(ctx, out->cz, f.cz, n);
-        d2h(ctx, out->maxball_mask, f.mask, n);
-        d2h(ctx, out->pore_labels, f.labels, n);
-        d2h(ctx, out->watershed_labels, f.labels_ws, n);
+    run_pore_chain(ctx, f, dims, o, out);
+    // The pore-stage fields are final here; with geodesics still to run, their copies go on
+    // the side stream and overlap the geodesic kernels (which neither read nor write them).
+    cudaStream_t cs = ctx->stream;
+    SideJoin join;
+    const bool any_pore_field = out->edt2 || out->crad2 || out->cx || out->cy || out->cz || out->maxball_mask ||
+                                out->pore_labels || out->watershed_labels;
+    if (o.run_pores && o.run_geodesic && any_pore_field) {
+        cs = ctx->side_stream();
+        join.ctx = ctx;
+        PMA_CUDA(cudaEventRecord(ctx->copy_event, ctx->stream));
+        PMA_CUDA(cudaStreamWaitEvent(cs, ctx->copy_event, 0));
     }
+    if (o.run_pores) {
+        d2h(cs, out->edt2, f.edt2, n);
+        d2h(cs, out->crad2, f.crad2, n);
+        d2h(cs, out->cx, f.cx, n);
+        d2h(cs, out->cy, f.cy, n);
+        d2h(cs, out->cz, f.cz, n);
+        d2h(cs, out->maxball_mask, f.mask, n);
+        d2h(cs, out->pore_labels, f.labels, n);
+        d2h(cs, out->watershed_labels, f.labels_ws, n);
+    }
+    run_geo_chain(ctx, f, dims, o, out);
     if (o.run_geodesic) {
-        d2h(ctx, out->dist_f32, f.dist32, n);
-        d2h(ctx, out->dist_f64, f.dist64, n);
-        d2h(ctx, out->cavity, f.cavity, n);
+        d2h(ctx->stream, out->dist_f32, f.dist32, n);
+        d2h(ctx->stream, out->dist_f64, f.dist64, n);
+        d2h(ctx->stream, out->cavity, f.cavity, n);
+    }
+    if (cs != ctx->stream) {  // the stream's later work must not reuse the fields before the copies end
+        PMA_CUDA(cudaEventRecord(ctx->copy_event, cs));
+        PMA_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_event, 0));
     }
     ctx->sync();
 }
@@ -145,7 +174,8 @@ void run_pipeline_device(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, co
         if (geo64) f.dist64 = pick(out->dist_f64, "pipe.dist64", n * 8);
         else f.dist32 = pick(out->dist_f32, "pipe.dist32", n * 4);
     }
-    run_chain(ctx, f, dims, o, out);
+    run_pore_chain(ctx, f, dims, o, out);
+    run_geo_chain(ctx, f, dims, o, out);
     ctx->sync();
 }
 

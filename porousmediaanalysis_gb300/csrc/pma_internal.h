@@ -93,6 +93,10 @@ struct pma_ctx {
         demand_bytes = 0;
     }
 
+    cudaStream_t copy_stream = nullptr;  // copies that overlap later kernels of the stream
+    cudaEvent_t copy_event = nullptr;
+    cudaStream_t side_stream();          // created on first use
+
     void* scratch(const std::string& tag, size_t bytes);
     void release(const std::string& tag);  // frees one scratch buffer (after the stream's work)
     void* host_staging(size_t bytes);

@@ -190,9 +190,10 @@ __device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t*
             s.pbound[pore] = 1;
         } else {
             const size_t w = s.g.idx(nx, ny, nz);
+            // both loads in flight at once; the claim is only used for a touched voxel
             const uint32_t r = __ldg(s.crad + w);
+            const uint32_t c = __ldcg(s.claim + w);
             if (r != 0 && r <= depth) {  // WC.cpp:152-156
-                const uint32_t c = __ldcg(s.claim + w);
                 if (c == 0) {
                     atomicMin(&s.ckey[w], (tag << 40) | seq);
                     touched = 1;
@@ -208,13 +209,15 @@ __device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t*
 // Returns true when the event stamps a same-depth claim (a node of the next generation).
 __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
                                                  unsigned long long seq, uint32_t depth, unsigned long long gen) {
-    if (!__ldcg(s.ev_touch + seq)) return false;
     const unsigned long long i = seq / 27;
     const int j = static_cast<int>(seq - i * 27);
-    int dx, dy, dz;
-    stencil_offset(j, s.d3q7, dx, dy, dz);
+    // the node (shared by the event's warp neighbours) is loaded along with the flag
+    const uint8_t touched = __ldcg(s.ev_touch + seq);
     const uint32_t v = __ldcg(gv + i);
     const uint32_t pore = __ldcg(gp + i);
+    if (!touched) return false;
+    int dx, dy, dz;
+    stencil_offset(j, s.d3q7, dx, dy, dz);
     // the neighbour is inside the box (phase 0 touched it)
     const size_t w = static_cast<size_t>(static_cast<long long>(v) +
                                          (static_cast<long long>(dz) * s.g.SX + dx) * s.g.SY + dy);
@@ -713,7 +716,9 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         PMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_generations, kChunk / 4, 0));
         PMA_REQUIRE(per_sm > 0, PMA_ERR_CUDA, "pma_watershed: generation kernel does not fit an SM");
         // sized to the largest frontier (about 16 events per thread and phase), so that the
-        // launches of small volumes leave the rest of the GPU to other streams (batch lanes)
+        // launches of small volumes leave the rest of the GPU to other streams (batch lanes).
+        // (Sizing each launch to its starting frontier instead, at about 4 events per thread,
+        // made barriers cheaper but the step slower: 950 -> 971 ms at 1024^3.)
         const size_t coop_need = (max_events + 16 * (kChunk / 4) - 1) / (16 * (kChunk / 4));
         const unsigned coop_grid = static_cast<unsigned>(
             std::max<size_t>(1, std::min<size_t>(coop_need, static_cast<size_t>(ctx->num_sms) * std::min(per_sm, 8))));
