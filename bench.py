@@ -45,8 +45,8 @@ WORKLOADS = {
 # DRAM bytes per voxel measured by ncu over all launches of a kernel in one step of a 320^3
 # GRF (profiles/), used as the roofline's `traffic` when that kernel dominates.
 TRAFFIC_PER_VOXEL = {
-    "ws_generations": (491.0, "ncu dram__bytes_read+write of all ws_generations launches of one 320^3 "
-                              "GRF step (profiles/ws_generations_grf320.md), scaled by voxels"),
+    "ws_generations": (338.0, "ncu dram__bytes_read+write of all ws_generations launches of one 320^3 "
+                              "GRF step (profiles/launches_grf320_pipeline.md), scaled by voxels"),
 }
 
 # Algorithmic HBM bytes per voxel of the timed kernels (reads + writes each kernel must do).
@@ -472,7 +472,9 @@ def main():
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    dom = max(kern.items(), key=lambda kv: kv[1][0]) if kern else ("none", (0.0, 1))
+    # whole-stage regions (stage_*) bracket the kernels; the dominant one is a kernel region
+    kk = {k: v for k, v in kern.items() if not k.startswith("stage_")}
+    dom = max(kk.items(), key=lambda kv: kv[1][0]) if kk else ("none", (0.0, 1))
     name, (tot_ms, nlaunch) = dom
     per_launch_ms = tot_ms / max(nlaunch, 1)
     units_per_launch = nvox * args.steps / max(nlaunch, 1)
