@@ -484,6 +484,7 @@ T* buf(pma_ctx* ctx, const char* tag, size_t count) {
 void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t max_edt2,
                       uint32_t* crad2, uint32_t* cx, uint32_t* cy, uint32_t* cz, uint8_t* mask,
                       uint64_t* count) {
+    KernelTimer kt_stage(ctx, "stage_balls");  // the whole stage, for the untimed remainder
     check_dims(d);
     PMA_REQUIRE(edt2 && crad2 && cx && cy && cz && mask, PMA_ERR_ARGUMENT,
                 "pma_containing_balls: null device pointer");

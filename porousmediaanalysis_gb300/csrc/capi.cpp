@@ -61,12 +61,6 @@ void* pma_ctx::scratch(const std::string& tag, size_t bytes) {
     return b.ptr;
 }
 
-cudaStream_t pma_ctx::side_stream() {
-    if (!copy_stream) PMA_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
-    if (!copy_event) PMA_CUDA(cudaEventCreateWithFlags(&copy_event, cudaEventDisableTiming));
-    return copy_stream;
-}
-
 void pma_ctx::release(const std::string& tag) {
     auto it = cache.find(tag);
     if (it == cache.end()) return;
@@ -158,11 +152,6 @@ int pma_ctx_destroy(pma_ctx* ctx) {
         cudaStreamSynchronize(ctx->stream);
         if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
         if (ctx->sync_event) cudaEventDestroy(ctx->sync_event);
-        if (ctx->copy_stream) {
-            cudaStreamSynchronize(ctx->copy_stream);
-            cudaStreamDestroy(ctx->copy_stream);
-        }
-        if (ctx->copy_event) cudaEventDestroy(ctx->copy_event);
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
         if (ctx->count_word) cudaFreeHost(ctx->count_word);
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);

@@ -138,4 +138,44 @@ inline std::vector<uint32_t> pore_id_sequence(size_t n) {
     return ids;
 }
 
+// Small device-to-host reads of loop counters: a one-block kernel stores the words straight
+// into pinned (mapped) host memory, then the stream is synchronised. Unlike cudaMemcpyAsync,
+// the read does not queue on a copy engine behind large transfers of other streams (the
+// pipeline's side-stream result copies), and one launch covers several sources.
+struct ReadBack {
+    const void* src[4];
+    void* dst[4];
+    unsigned words[4];  // 4-byte words
+    int n = 0;
+    void add(void* host_dst, const void* dev_src, size_t bytes) {
+        src[n] = dev_src;
+        dst[n] = host_dst;
+        words[n] = static_cast<unsigned>(bytes / 4);
+        ++n;
+    }
+};
+
+namespace {  // one copy per translation unit
+
+__global__ void read_back_kernel(ReadBack rb) {
+    for (int k = 0; k < rb.n; ++k)
+        for (unsigned i = threadIdx.x; i < rb.words[k]; i += blockDim.x)
+            static_cast<volatile uint32_t*>(rb.dst[k])[i] = __ldcg(static_cast<const uint32_t*>(rb.src[k]) + i);
+    __threadfence_system();
+}
+
+inline void read_back(pma_ctx* ctx, ReadBack rb) {
+    for (int k = 0; k < rb.n; ++k) {
+        void* d = nullptr;
+        PMA_CUDA(cudaHostGetDevicePointer(&d, rb.dst[k], 0));
+        rb.dst[k] = d;
+    }
+    read_back_kernel<<<1, 64, 0, ctx->stream>>>(rb);
+    ctx->count_launch();
+    ctx->check_launch("read_back");
+    ctx->sync();
+}
+
+}  // namespace
+
 }  // namespace pma

@@ -206,6 +206,7 @@ void edt_smem_attributes(size_t optin) {
 
 void edt(pma_ctx* ctx, const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats* stats,
          uint64_t* h_hist, size_t hist_cap) {
+    KernelTimer kt_stage(ctx, "stage_edt");  // the whole stage, for the untimed remainder
     check_dims(d);
     edt_smem_attributes(ctx->smem_optin);
     PMA_REQUIRE(solid && edt2, PMA_ERR_ARGUMENT, "pma_edt: null device pointer");

@@ -15,7 +15,7 @@
 // b); before its sweep, bucket k's bitmap is compacted into a list in voxel order (per block
 // of 8192 voxels), which is also cleared for bucket k + 4. A voxel whose distance dropped to a
 // lower bucket after being set is skipped as stale.
-#include "pma_internal.h"
+#include "devutil.cuh"
 
 #include <cfloat>
 #include <cmath>
@@ -257,6 +257,7 @@ __global__ void geo_shell_search(const uint8_t* __restrict__ solid, const T* __r
 template <class T>
 int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
              uint32_t* cavity, pma_cavity* cav, int cav_cap) {
+    KernelTimer kt_stage(ctx, "stage_geodesic");  // the whole stage, for the untimed remainder
     check_dims(d);
     PMA_REQUIRE(solid && dist && cavity, PMA_ERR_ARGUMENT, "pma_geodesic: null device pointer");
     cudaStream_t s = ctx->stream;
@@ -376,8 +377,11 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
             }
             ctx->count_launch(3 * max_buckets_per_sync - 1);
             ctx->check_launch("geo_bucket");
-            PMA_CUDA(cudaMemcpyAsync(h, misc, 3 * 8, cudaMemcpyDeviceToHost, s));
-            ctx->sync();
+            {
+                ReadBack rb;
+                rb.add(h, misc, 3 * 8);
+                read_back(ctx, rb);
+            }
             const unsigned* cnt = reinterpret_cast<const unsigned*>(h);
             PMA_REQUIRE(reinterpret_cast<const unsigned*>(h)[4] == 0, PMA_ERR_LIMIT,
                         "geodesic: frontier list overflow");
@@ -387,8 +391,11 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
             PMA_REQUIRE(static_cast<size_t>(k) <= 2 * n + 64, PMA_ERR_LIMIT,
                         "geodesic: bucket sweep did not terminate");
         }
-        PMA_CUDA(cudaMemcpyAsync(h, misc, 5 * 8, cudaMemcpyDeviceToHost, s));
-        ctx->sync();
+        {
+            ReadBack rb;
+            rb.add(h, misc, 5 * 8);
+            read_back(ctx, rb);
+        }
         const unsigned walls_bits = static_cast<unsigned>(h[3]);
         const unsigned long long settled = h[4];
         const int reached = __builtin_popcount(walls_bits);

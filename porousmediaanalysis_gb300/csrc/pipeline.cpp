@@ -57,15 +57,6 @@ void d2h(cudaStream_t s, T* host, const T* dev, size_t n) {
     if (host && dev) PMA_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, s));
 }
 
-// Waits for the context's side stream on every exit, so that no copy into the caller's
-// buffers is left running when the call returns (an error included).
-struct SideJoin {
-    pma_ctx* ctx = nullptr;
-    ~SideJoin() {
-        if (ctx) cudaStreamSynchronize(ctx->copy_stream);
-    }
-};
-
 }  // namespace
 }  // namespace pma
 
@@ -111,37 +102,25 @@ void run_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims, cons
     if (geo64) f.cavity = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
     PMA_CUDA(cudaMemcpyAsync(f.solid, h_solid, n, cudaMemcpyHostToDevice, ctx->stream));
     run_pore_chain(ctx, f, dims, o, out);
-    // The pore-stage fields are final here; with geodesics still to run, their copies go on
-    // the side stream and overlap the geodesic kernels (which neither read nor write them).
-    cudaStream_t cs = ctx->stream;
-    SideJoin join;
-    const bool any_pore_field = out->edt2 || out->crad2 || out->cx || out->cy || out->cz || out->maxball_mask ||
-                                out->pore_labels || out->watershed_labels;
-    if (o.run_pores && o.run_geodesic && any_pore_field) {
-        cs = ctx->side_stream();
-        join.ctx = ctx;
-        PMA_CUDA(cudaEventRecord(ctx->copy_event, ctx->stream));
-        PMA_CUDA(cudaStreamWaitEvent(cs, ctx->copy_event, 0));
-    }
-    if (o.run_pores) {
-        d2h(cs, out->edt2, f.edt2, n);
-        d2h(cs, out->crad2, f.crad2, n);
-        d2h(cs, out->cx, f.cx, n);
-        d2h(cs, out->cy, f.cy, n);
-        d2h(cs, out->cz, f.cz, n);
-        d2h(cs, out->maxball_mask, f.mask, n);
-        d2h(cs, out->pore_labels, f.labels, n);
-        d2h(cs, out->watershed_labels, f.labels_ws, n);
-    }
     run_geo_chain(ctx, f, dims, o, out);
+    // Results go back after the whole chain. (Copying the pore-stage fields on a second
+    // stream while the geodesics ran made the geodesic kernels slower, 337 -> 754 ms at 1024^3,
+    // by more than the copy itself costs: the copy into the caller's pinned buffer and the
+    // geodesics' random accesses compete for address translation.)
+    if (o.run_pores) {
+        d2h(ctx->stream, out->edt2, f.edt2, n);
+        d2h(ctx->stream, out->crad2, f.crad2, n);
+        d2h(ctx->stream, out->cx, f.cx, n);
+        d2h(ctx->stream, out->cy, f.cy, n);
+        d2h(ctx->stream, out->cz, f.cz, n);
+        d2h(ctx->stream, out->maxball_mask, f.mask, n);
+        d2h(ctx->stream, out->pore_labels, f.labels, n);
+        d2h(ctx->stream, out->watershed_labels, f.labels_ws, n);
+    }
     if (o.run_geodesic) {
         d2h(ctx->stream, out->dist_f32, f.dist32, n);
         d2h(ctx->stream, out->dist_f64, f.dist64, n);
         d2h(ctx->stream, out->cavity, f.cavity, n);
-    }
-    if (cs != ctx->stream) {  // the stream's later work must not reuse the fields before the copies end
-        PMA_CUDA(cudaEventRecord(ctx->copy_event, cs));
-        PMA_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_event, 0));
     }
     ctx->sync();
 }

@@ -93,11 +93,11 @@ struct pma_ctx {
         demand_bytes = 0;
     }
 
-    cudaStream_t copy_stream = nullptr;  // copies that overlap later kernels of the stream
-    cudaEvent_t copy_event = nullptr;
-    cudaStream_t side_stream();          // created on first use
-
     void* scratch(const std::string& tag, size_t bytes);
+    size_t cached_bytes(const std::string& tag) const {  // capacity held under tag (0 = none)
+        auto it = cache.find(tag);
+        return it == cache.end() ? 0 : it->second.bytes;
+    }
     void release(const std::string& tag);  // frees one scratch buffer (after the stream's work)
     void* host_staging(size_t bytes);
     int64_t* pinned_count();  // a pinned word of its own for counts read back after CUB calls

@@ -201,6 +201,112 @@ __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int
     }
 }
 
+// Large volumes, after the pointer jumps: almost every voxel points at its initial tree's
+// root, so a neighbour pair of equal crad whose parents differ is the rare case. uf_pairs
+// records those parent pairs (de-duplicated within the block's voxels) instead of walking to
+// the roots in line, and uf_union_pairs unions them, one thread per pair, so that the root
+// walks (into arrays far larger than L2) run in parallel rather than one neighbour after
+// another. The partition and its roots are the same: each plateau's root is its smallest
+// voxel index, whatever the union order.
+constexpr int kPairTable = 2048;
+
+__global__ void uf_pairs(const uint32_t* __restrict__ crad, Grid g, size_t n, int d3q7,
+                         const uint32_t* __restrict__ parent, unsigned long long* __restrict__ pairs,
+                         unsigned long long cap, unsigned long long* __restrict__ count) {
+    __shared__ unsigned long long table[kPairTable];
+    const unsigned lane = threadIdx.x & 31;
+    // block-uniform trip count: whole blocks reach the barriers and warps the placement below
+    for (size_t base = static_cast<size_t>(blockIdx.x) * blockDim.x; base < n;
+         base += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t v = base + threadIdx.x;
+        const uint32_t r = v < n ? crad[v] : 0u;
+        // shared-memory set of the block's pairs: keep the first copy of each
+        for (int i = threadIdx.x; i < kPairTable; i += blockDim.x) table[i] = ~0ull;
+        __syncthreads();
+        unsigned long long keys[13];
+        int kept = 0;
+        if (r) {
+            int x, y, z;
+            g.coords(v, x, y, z);
+            const uint32_t rv = parent[v];
+            uint32_t seen[13];
+            int ns = 0;
+            for (int k = 0; k < 13; ++k) {  // the 13 forward offsets, as in uf_hook
+                int dx, dy, dz;
+                if (k < 4) {
+                    dz = 0;
+                    dx = (k == 0) ? 0 : 1;
+                    dy = (k == 0) ? 1 : k - 2;
+                } else {
+                    dz = 1;
+                    dx = (k - 4) / 3 - 1;
+                    dy = (k - 4) % 3 - 1;
+                }
+                if (d3q7 && (dx != 0) + (dy != 0) + (dz != 0) > 1) continue;
+                const int nx = x + dx, ny = y + dy, nz = z + dz;
+                if (!g.inside(nx, ny, nz)) continue;
+                const size_t w = g.idx(nx, ny, nz);
+                if (crad[w] != r) continue;
+                const uint32_t pw = parent[w];
+                if (pw == rv) continue;  // already in one tree
+                bool dup = false;
+                for (int i = 0; i < ns; ++i) dup |= seen[i] == pw;
+                if (dup) continue;
+                seen[ns++] = pw;
+                const uint32_t lo = min(rv, pw), hi = max(rv, pw);
+                const unsigned long long key = (static_cast<unsigned long long>(lo) << 32) | hi;
+                unsigned h = static_cast<unsigned>((key * 0x9E3779B97F4A7C15ull) >> 40) & (kPairTable - 1);
+                bool fresh = true;
+                for (int probe = 0; probe < 8; ++probe, h = (h + 1) & (kPairTable - 1)) {
+                    const unsigned long long prev = atomicCAS(&table[h], ~0ull, key);
+                    if (prev == ~0ull) break;
+                    if (prev == key) {
+                        fresh = false;
+                        break;
+                    }
+                }
+                if (fresh) keys[kept++] = key;
+            }
+        }
+        __syncthreads();
+        // one atomic per warp; lanes place their pairs by a warp prefix sum
+        unsigned incl = static_cast<unsigned>(kept);
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<unsigned>(o)) incl += t;
+        }
+        unsigned long long pos = 0;
+        if (lane == 31 && incl) pos = atomicAdd(count, static_cast<unsigned long long>(incl));
+        pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + (incl - static_cast<unsigned>(kept));
+        for (int i = 0; i < kept; ++i)
+            if (pos + i < cap) pairs[pos + i] = keys[i];
+    }
+}
+
+__global__ void uf_union_pairs(const unsigned long long* __restrict__ pairs, size_t np,
+                               uint32_t* __restrict__ parent, unsigned int* __restrict__ err) {
+    PMA_GRID_STRIDE(i, np) {
+        uint32_t a = uf_root(parent, static_cast<uint32_t>(pairs[i] >> 32));
+        uint32_t b = uf_root(parent, static_cast<uint32_t>(pairs[i]));
+        int it = 0;
+        while (a != b) {
+            if (++it > kUnionLimit) {
+                atomicOr(err, 1u);
+                break;
+            }
+            if (a < b) {
+                const uint32_t old = atomicCAS(&parent[b], b, a);
+                if (old == b) break;
+                b = old;
+            } else {
+                const uint32_t old = atomicCAS(&parent[a], a, b);
+                if (old == a) break;
+                a = old;
+            }
+        }
+    }
+}
+
 // Read-only root walk: flattening must not halve paths, or a racing halving store could
 // replace another voxel's final root pointer with an intermediate ancestor.
 __device__ __forceinline__ uint32_t uf_root_readonly(const uint32_t* parent, uint32_t v) {
@@ -263,16 +369,15 @@ __global__ void plateau_stats(const uint32_t* __restrict__ pid, const uint32_t* 
     }
 }
 
-// Plateau edges q -> p (crad strictly decreasing), deduplicated per voxel.
+// Plateau edges q -> p (crad strictly decreasing), deduplicated per voxel and per block;
+// count receives the number of edges, also those beyond cap (not written).
 constexpr int kEdgeTable = 2048;  // shared-memory pair set of plateau_edges (power of two)
 
-template <bool kWrite>
 __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
                               Grid g, size_t n, int d3q7, unsigned long long* __restrict__ count,
                               unsigned long long* __restrict__ edges, unsigned long long cap) {
-    unsigned long long local = 0;
     const unsigned lane = threadIdx.x & 31;
-    __shared__ unsigned long long table[kWrite ? kEdgeTable : 1];
+    __shared__ unsigned long long table[kEdgeTable];
     // block-uniform trip count, so whole warps reach the warp-wide placement below
     for (size_t base = static_cast<size_t>(blockIdx.x) * blockDim.x; base < n;
          base += static_cast<size_t>(gridDim.x) * blockDim.x) {
@@ -299,7 +404,7 @@ __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* 
                 seen[ns++] = q;
             }
         }
-        if (kWrite) {
+        {
             // Neighbouring voxels mostly report the same plateau pairs: keep the first copy
             // of each pair within the block's 256 voxels (shared-memory hash set; a pair that
             // finds no free slot is kept too - the sort and unique that follow are exact).
@@ -333,13 +438,7 @@ __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* 
             pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + (incl - static_cast<unsigned>(ns));
             for (int i = 0; i < ns; ++i)
                 if (pos + i < cap) edges[pos + i] = (static_cast<unsigned long long>(seen[i]) << 32) | p;
-        } else {
-            local += ns;
         }
-    }
-    if (!kWrite) {
-        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
-        if (lane == 0 && local) atomicAdd(count, local);
     }
 }
 
@@ -942,6 +1041,7 @@ T* buf(pma_ctx* ctx, const char* tag, size_t count) {
 
 pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const uint32_t* crad2,
                  pma_dims d, pma_stencil st, uint32_t* labels) {
+    KernelTimer kt_stage(ctx, "stage_pores");  // the whole stage, for the untimed remainder
     check_dims(d);
     PMA_REQUIRE(mask && edt2 && crad2 && labels, PMA_ERR_ARGUMENT, "pma_pores: null device pointer");
     cudaStream_t s = ctx->stream;
@@ -994,7 +1094,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     uf_init<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid);
     ctx->check_launch("uf_init");
     {
-        KernelTimer kt(ctx, "uf_hook");
+        KernelTimer kt(ctx, "uf_jump");
         if (n >= kJumpMinVoxels) {
             unsigned int* changed =
                 reinterpret_cast<unsigned int*>(buf<unsigned long long>(ctx, "pores.jump", kJumpPasses));
@@ -1003,7 +1103,34 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             ctx->count_launch(kJumpPasses - 1);
             ctx->check_launch("uf_jump");
         }
-        uf_hook<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid, err);
+    }
+    {
+        KernelTimer kt(ctx, "uf_hook");
+        if (n >= kJumpMinVoxels) {
+            // parent pairs, then their unions (the buffer grows to what a call needed)
+            auto* pcount = reinterpret_cast<unsigned long long*>(d_count + 1);  // free until the edges
+            unsigned long long pcap = std::max<unsigned long long>(
+                std::max<unsigned long long>(n / 64, 1ull << 20), ctx->cached_bytes("pores.uf_pairs") / 8);
+            unsigned long long npairs = 0;
+            unsigned long long* pairs = nullptr;
+            for (int attempt = 0;; ++attempt) {
+                pairs = buf<unsigned long long>(ctx, "pores.uf_pairs", pcap);
+                PMA_CUDA(cudaMemsetAsync(pcount, 0, 8, s));
+                uf_pairs<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid, pairs, pcap, pcount);
+                ctx->check_launch("uf_pairs");
+                PMA_CUDA(cudaMemcpyAsync(&npairs, pcount, 8, cudaMemcpyDeviceToHost, s));
+                ctx->sync();
+                if (npairs <= pcap) break;
+                PMA_REQUIRE(attempt < 3, PMA_ERR_INTERNAL, "pma_pores: plateau pair count did not settle");
+                pcap = npairs + npairs / 8 + 1024;
+            }
+            if (npairs) {
+                uf_union_pairs<<<grid_for(ctx, npairs), 256, 0, s>>>(pairs, npairs, pid, err);
+                ctx->check_launch("uf_union_pairs");
+            }
+        } else {
+            uf_hook<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid, err);
+        }
     }
     ctx->check_launch("uf_hook");
     uf_flatten<<<G, 256, 0, s>>>(n, pid);
@@ -1026,29 +1153,30 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     // Edges between plateaus, sorted by destination.
     auto kt_edges = std::make_unique<KernelTimer>(ctx, "plateau_edges");
     auto* ecount = reinterpret_cast<unsigned long long*>(d_count + 1);
-    PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
-    {
-        KernelTimer kt(ctx, "edges_count");
-        plateau_edges<false><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, nullptr, 0);
-    }
-    ctx->check_launch("plateau_edges(count)");
-    unsigned long long ne_raw = 0;
-    PMA_CUDA(cudaMemcpyAsync(&ne_raw, ecount, 8, cudaMemcpyDeviceToHost, s));
-    ctx->sync();
-    auto* edges_raw = buf<unsigned long long>(ctx, "pores.edges_raw", ne_raw);
-    PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
-    {
-        KernelTimer kt(ctx, "edges_write");
-        plateau_edges<true><<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, edges_raw, ne_raw);
-    }
-    ctx->check_launch("plateau_edges(write)");
-    // Keys are (destination << 32 | source): sorting groups the predecessors of each plateau.
-    int64_t ne = 0;
-    if (ne_raw) {
-        unsigned long long ne_kept = 0;  // after the per-block de-duplication
+    // One pass writes the edges into a buffer of at least n/8 entries, or of what an earlier
+    // call needed (the edges kept after the per-block de-duplication are far fewer than the
+    // voxels); when they do not fit, the pass is repeated with the size it counted.
+    unsigned long long ecap = std::max<unsigned long long>(
+        std::max<unsigned long long>(n / 8, 1ull << 20), ctx->cached_bytes("pores.edges_raw") / 8);
+    unsigned long long* edges_raw = nullptr;
+    unsigned long long ne_kept = 0;
+    for (int attempt = 0;; ++attempt) {
+        edges_raw = buf<unsigned long long>(ctx, "pores.edges_raw", ecap);
+        PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
+        {
+            KernelTimer kt(ctx, "edges_write");
+            plateau_edges<<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, edges_raw, ecap);
+        }
+        ctx->check_launch("plateau_edges");
         PMA_CUDA(cudaMemcpyAsync(&ne_kept, ecount, 8, cudaMemcpyDeviceToHost, s));
         ctx->sync();
-        ne_kept = std::min(ne_kept, ne_raw);
+        if (ne_kept <= ecap) break;
+        PMA_REQUIRE(attempt < 3, PMA_ERR_INTERNAL, "pma_pores: plateau edge count did not settle");
+        ecap = ne_kept + ne_kept / 8 + 1024;
+    }
+    // Keys are (destination << 32 | source): sorting groups the predecessors of each plateau.
+    int64_t ne = 0;
+    if (ne_kept) {
         auto* edges = buf<unsigned long long>(ctx, "pores.edges", ne_kept);
         sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_kept));
         ne = unique(ctx, edges, edges_raw, static_cast<int64_t>(ne_kept), d_count);
@@ -1147,8 +1275,11 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                 level_heavy<<<heavy_grid, 512, 0, s>>>(ps, b);
                 ctx->count_launch(2);
             }
-            PMA_CUDA(cudaMemcpyAsync(h_info, ps.info, 32, cudaMemcpyDeviceToHost, s));
-            ctx->sync();
+            {
+                ReadBack rb;
+                rb.add(h_info, ps.info, 32);
+                read_back(ctx, rb);
+            }
             const unsigned long long nbig = h_info[1], total = h_info[2];
             int64_t merged = 0;
             int shift = 32;
@@ -1170,8 +1301,9 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                 while ((1ull << big_bits) < nbig) ++big_bits;
                 narrow = rank_bits < 32 && rank_bits + big_bits <= 32;
                 auto read_emitted = [&]() {
-                    PMA_CUDA(cudaMemcpyAsync(h_info, ps.info, 32, cudaMemcpyDeviceToHost, s));
-                    ctx->sync();
+                    ReadBack rb;
+                    rb.add(h_info, ps.info, 32);
+                    read_back(ctx, rb);
                     return static_cast<int64_t>(std::min<unsigned long long>(h_info[3], total));
                 };
                 auto* deg = buf<unsigned long long>(ctx, "pores.bdeg", nbig);
@@ -1459,6 +1591,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
 
 // a11: EmptyPoresRemover.cpp:31-244 on the host table, then one relabel launch.
 void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d) {
+    KernelTimer kt_stage(ctx, "stage_removal");
     check_dims(d);
     PMA_REQUIRE(labels, PMA_ERR_ARGUMENT, "pma_remove_empty_pores: null labels");
     // EPR.cpp:193-244: drop zero-volume pores and remove them from the type lists.

@@ -18,8 +18,8 @@
 //              which is sorted by time when that depth starts; in the same pass, touches by
 //              pores other than the voxel's owner record, per voxel and pore, their first
 //              touch time (extensions).
-// Frontier sizes stay on the device; the next generation is compacted in event order by a
-// count / scan / scatter over event slots stamped with the generation number.
+// Frontier sizes stay on the device; the next generation is compacted in event order (see
+// ws_generations).
 //
 // Shared types: a voxel's key is its claimer plus its extending pores in time order; every
 // prefix of length >= 2 was created at the time of its last extension. All prefixes are
@@ -206,9 +206,11 @@ __device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t*
     s.ev_touch[seq] = touched;
 }
 
-// Returns true when the event stamps a same-depth claim (a node of the next generation).
+// Returns true when the event claims a voxel of the same depth (a node of the next
+// generation: voxel nw of pore np_out).
 __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
-                                                 unsigned long long seq, uint32_t depth, unsigned long long gen) {
+                                                 unsigned long long seq, uint32_t depth, unsigned long long gen,
+                                                 uint32_t& nw, uint32_t& np_out) {
     const unsigned long long i = seq / 27;
     const int j = static_cast<int>(seq - i * 27);
     // the node (shared by the event's warp neighbours) is loaded along with the flag
@@ -226,8 +228,8 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
         s.claim[w] = pore + 1;
         const uint32_t r = __ldg(s.crad + w);
         if (r == depth) {
-            s.slot_voxel[seq] = static_cast<uint32_t>(w);
-            s.slot_gen[seq] = static_cast<uint32_t>(gen);
+            nw = static_cast<uint32_t>(w);
+            np_out = pore;
             return true;
         }
         const unsigned pos = atomicAdd(&s.bfill[r], 1u);
@@ -242,9 +244,65 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
     return false;
 }
 
-// Ordered compaction of a generation's same-depth claims (event slots stamped with the
-// generation number), in three steps: counts per chunk of kChunk slots (made by phase 1), an
-// exclusive scan of the counts (block 0), and the scatter of the claims in event order.
+// Ordered compaction of a generation's same-depth claims into the next frontier, in event
+// order. Two forms:
+//  * small generations (up to kLookbackChunks chunks of kChunk events) compact inside the
+//    resolve phase: each chunk (one block, four events per thread) ranks its claims, and its
+//    offset comes from a decoupled look-back over the chunks before it, read 32 descriptors at
+//    a time by one warp. A descriptor holds (generation << 40) | state << 38 | count, state
+//    1 = the chunk's own count, 2 = the inclusive prefix; one of an older generation is not
+//    yet published. Chunks publish their own count before looking back and every block of
+//    the cooperative grid is resident, so the look-back always ends; it is bounded all the
+//    same (err bit 16). This saves two of the four grid-wide barriers of a generation.
+//  * larger ones stamp their claims into event slots (generation number and voxel), count
+//    them per chunk, and compact in two more phases: an exclusive scan of the chunk counts
+//    (block 0) and the scatter of the stamped slots.
+// (The look-back alone serialises the chunks of a large generation: 907 -> 1108 ms per
+// 1024^3 step when every generation used it.)
+constexpr unsigned long long kDescOwn = 1ull << 38;
+constexpr unsigned long long kDescIncl = 2ull << 38;
+constexpr unsigned long long kDescVal = (1ull << 38) - 1;
+constexpr unsigned long long kLookbackChunks = 256;
+
+// Called by all 32 lanes of one warp; returns the exclusive prefix of chunk c.
+__device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned long long c, unsigned long long gen,
+                                          unsigned long long own, unsigned int* err, unsigned lane) {
+    volatile unsigned long long* vd = desc;
+    const unsigned long long tg = gen << 40;
+    if (lane == 0) vd[c] = tg | (c == 0 ? kDescIncl : kDescOwn) | own;
+    if (c == 0) return 0;
+    __threadfence();
+    unsigned long long excl = 0;
+    long long top = static_cast<long long>(c) - 1;
+    int spins = 0;
+    while (true) {
+        const long long p = top - static_cast<long long>(lane);
+        const bool valid = p >= 0;
+        const unsigned long long d = valid ? vd[p] : 0ull;
+        const bool ready = !valid || (d >> 40) == gen;
+        if (!__all_sync(0xFFFFFFFFu, ready)) {  // a predecessor has not published yet
+            if (++spins > kSpinLimit) {
+                if (lane == 0) atomicOr(err, 16u);
+                break;
+            }
+            continue;
+        }
+        // the nearest inclusive prefix ends the walk; owns before it are added
+        const unsigned incl = __ballot_sync(0xFFFFFFFFu, valid && (d & kDescIncl) != 0);
+        const int stop = incl ? __ffs(incl) - 1 : 31;
+        unsigned long long v = (valid && static_cast<int>(lane) <= stop) ? (d & kDescVal) : 0ull;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        excl += v;
+        if (incl || top < 32) break;  // chunk 0 is always inclusive
+        top -= 32;
+    }
+    if (lane == 0) {
+        __threadfence();
+        vd[c] = tg | kDescIncl | (excl + own);
+    }
+    return excl;
+}
+
 __device__ __forceinline__ void ws_slot_scan(unsigned int* ccount, unsigned long long nev, unsigned int* ng_next,
                                              unsigned int* part) {
     const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
@@ -326,15 +384,17 @@ __device__ __forceinline__ void ws_slot_scatter(const uint32_t* slot_gen, const 
 // Up to max_gens generations of one depth in a single cooperative launch, with grid-wide
 // barriers between the phases. ng[2] holds the two frontier sizes; the frontier starts on
 // side `cur`. out[0] = generations run, out[1] = the side holding the next frontier.
-__global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t* gv0, uint32_t* gp0, uint32_t* gv1,
+__global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint32_t* gv0, uint32_t* gp0, uint32_t* gv1,
                                                              uint32_t* gp1, unsigned int* ng, unsigned int* ccount,
-                                                             uint32_t depth, unsigned long long gen0, int max_gens,
-                                                             int cur, unsigned long long* out) {
+                                                             unsigned long long* desc, uint32_t depth,
+                                                             unsigned long long gen0, int max_gens, int cur,
+                                                             unsigned long long* out) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     __shared__ unsigned int part[kChunk / 4];
     const unsigned long long tid = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
     const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, lt = (1u << lane) - 1u;
     unsigned long long gen = gen0;
     int it = 0;
     for (; it < max_gens; ++it) {
@@ -348,30 +408,65 @@ __global__ void __launch_bounds__(kChunk / 4) ws_generations(WsState s, uint32_t
         const unsigned long long tag = kMaxGen - gen;
         for (unsigned long long seq = tid; seq < nev; seq += stride) ws_claim_event(s, gv, gp, seq, depth, gen, tag);
         grid.sync();
-        // Phase 1 by chunks of kChunk events (4 per thread), so that each block also counts
-        // its chunk's same-depth claims for the compaction.
+        // Resolve by chunks of kChunk events: event k * blockDim + t of a chunk is thread t's
+        // k-th, so event order is k-major, then thread.
         const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
+        const bool fused = nchunks <= kLookbackChunks;  // the same for every block
         for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-            unsigned int local = 0;
+            bool f[4];
+            uint32_t wv[4], wp[4];
+            unsigned m[4];
+#pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const unsigned long long seq = c * kChunk + k * (kChunk / 4) + threadIdx.x;
-                if (seq < nev && ws_resolve_event(s, gv, gp, seq, depth, gen)) ++local;
-            }
-            for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, o);
-            if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = local;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                unsigned int sum = 0;
-                for (unsigned w = 0; w < blockDim.x / 32; ++w) sum += part[w];
-                ccount[c] = sum;
+                f[k] = seq < nev && ws_resolve_event(s, gv, gp, seq, depth, gen, wv[k], wp[k]);
+                if (!fused && f[k]) {
+                    s.slot_voxel[seq] = wv[k];
+                    s.slot_gen[seq] = static_cast<uint32_t>(gen);
+                }
+                m[k] = __ballot_sync(0xFFFFFFFFu, f[k]);
+                if (lane == 0) part[k * (kChunk / 128) + warp] = __popc(m[k]);
             }
             __syncthreads();
+            if (warp == 0) {  // 4 rounds x 8 warps = 32 counts in event order
+                const unsigned v = part[lane];
+                unsigned incl = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned t2 = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= static_cast<unsigned>(o)) incl += t2;
+                }
+                const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                if (fused) {
+                    part[lane] = incl - v;
+                    const unsigned long long base = ws_lookback(desc, c, gen, total, s.err, lane);
+                    if (lane == 0) {
+                        part[32] = static_cast<unsigned int>(base);
+                        if (c == nchunks - 1) ng[cur ^ 1] = static_cast<unsigned int>(base + total);
+                    }
+                } else if (lane == 0) {
+                    ccount[c] = total;
+                }
+            }
+            __syncthreads();
+            if (fused) {
+                const unsigned base = part[32];
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (f[k]) {
+                        const unsigned pos = base + part[k * (kChunk / 128) + warp] + __popc(m[k] & lt);
+                        nv[pos] = wv[k];
+                        np_[pos] = wp[k];
+                    }
+                __syncthreads();  // part is reused by the next chunk
+            }
         }
         grid.sync();
-        if (blockIdx.x == 0) ws_slot_scan(ccount, nev, ng + (cur ^ 1), part);
-        grid.sync();
-        ws_slot_scatter(s.slot_gen, s.slot_voxel, nev, static_cast<uint32_t>(gen), ccount, gp, nv, np_, part);
-        grid.sync();
+        if (!fused) {
+            if (blockIdx.x == 0) ws_slot_scan(ccount, nev, ng + (cur ^ 1), part);
+            grid.sync();
+            ws_slot_scatter(s.slot_gen, s.slot_voxel, nev, static_cast<uint32_t>(gen), ccount, gp, nv, np_, part);
+            grid.sync();
+        }
         cur ^= 1;
     }
     if (tid == 0) {
@@ -576,6 +671,7 @@ T* buf(pma_ctx* ctx, const char* tag, size_t count) {
 
 pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, pma_dims d,
                      pma_stencil st, uint32_t max_edt2, uint32_t* labels) {
+    KernelTimer kt_stage(ctx, "stage_watershed");  // the whole stage, for the untimed remainder
     check_dims(d);
     PMA_REQUIRE(crad2 && labels, PMA_ERR_ARGUMENT, "pma_watershed: null device pointer");
     cudaStream_t s = ctx->stream;
@@ -680,11 +776,17 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         auto* srt_time = buf<unsigned long long>(ctx, "ws.srt_time", max_bucket);
         auto* srt_val = buf<unsigned long long>(ctx, "ws.srt_val", max_bucket);
         const size_t max_events = max_bucket * 27;
+
+        ws.ev_touch = buf<uint8_t>(ctx, "ws.ev_touch", max_events);  // written for every event by phase 0
+        // frontier compaction: event slots and chunk counts (large generations), chunk
+        // descriptors (small ones); generations restart at 1 in this attempt
         ws.slot_gen = buf<uint32_t>(ctx, "ws.slot_gen", max_events);
         ws.slot_voxel = buf<uint32_t>(ctx, "ws.slot_voxel", max_events);
-        ws.ev_touch = buf<uint8_t>(ctx, "ws.ev_touch", max_events);  // written for every event by phase 0
-        PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));  // generations start at 1
-        unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", (max_events + kChunk - 1) / kChunk);
+        PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));
+        const size_t max_chunks = (max_events + kChunk - 1) / kChunk;
+        unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", max_chunks);
+        auto* desc = buf<unsigned long long>(ctx, "ws.desc", std::min<size_t>(max_chunks, kLookbackChunks));
+        PMA_CUDA(cudaMemsetAsync(desc, 0, std::min<size_t>(max_chunks, kLookbackChunks) * 8, s));
         PMA_CUDA(cudaMemcpyAsync(d_boff, boff.data(), (nb + 1) * 8ull, cudaMemcpyHostToDevice, s));
         std::vector<unsigned int> h_fill(nb, 0);
         if (npores) {
@@ -735,9 +837,10 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         for (size_t di = 0; di < depths.size(); ++di) {
             const int64_t depth = depths[di];
             if (!have_count) {
-                PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + depth, 4, cudaMemcpyDeviceToHost, s));
-                PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
-                ctx->sync();
+                ReadBack rb;
+                rb.add(h_small, ws.bfill + depth, 4);
+                rb.add(h_small + 4, ws.ext_count, 4);
+                read_back(ctx, rb);
                 grow_records(h_small[4]);
                 n0 = h_small[0];
             }
@@ -761,18 +864,20 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
             while (true) {
                 const uint32_t dep = static_cast<uint32_t>(depth);
                 int gens = kGensPerLaunch;
-                void* args[] = {&ws, &gvb[0], &gpb[0], &gvb[1], &gpb[1], &d_ng, &ccount,
+                void* args[] = {&ws, &gvb[0], &gpb[0], &gvb[1], &gpb[1], &d_ng, &ccount, &desc,
                                 const_cast<uint32_t*>(&dep), &gen, &gens, &cur, &d_out};
                 PMA_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ws_generations), coop_grid,
                                                      kChunk / 4, args, 0, s));
                 ctx->count_launch(1);
-                PMA_CUDA(cudaMemcpyAsync(h_out, d_out, 16, cudaMemcpyDeviceToHost, s));
-                PMA_CUDA(cudaMemcpyAsync(h_small + 4, ws.ext_count, 4, cudaMemcpyDeviceToHost, s));
-                PMA_CUDA(cudaMemcpyAsync(h_small + 6, d_ng, 8, cudaMemcpyDeviceToHost, s));
-                // the next depth's entries are final once this depth is done: read them along
-                if (next_depth >= 0)
-                    PMA_CUDA(cudaMemcpyAsync(h_small, ws.bfill + next_depth, 4, cudaMemcpyDeviceToHost, s));
-                ctx->sync();
+                {
+                    ReadBack rb;
+                    rb.add(h_out, d_out, 16);
+                    rb.add(h_small + 4, ws.ext_count, 4);
+                    rb.add(h_small + 6, d_ng, 8);
+                    // the next depth's entries are final once this depth is done: read them along
+                    if (next_depth >= 0) rb.add(h_small, ws.bfill + next_depth, 4);
+                    read_back(ctx, rb);
+                }
                 gen += h_out[0];
                 cur = static_cast<int>(h_out[1]);
                 grow_records(h_small[4]);
@@ -792,6 +897,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     }
     PMA_REQUIRE(!(h_err & 2u), PMA_ERR_LIMIT, "pma_watershed: more than 7 pores touch one voxel");
     PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
+    PMA_REQUIRE(!(h_err & 16u), PMA_ERR_LIMIT, "pma_watershed: frontier compaction look-back did not finish");
 
     // Volumes, labels and shared voxels.
     auto* pvol = buf<unsigned long long>(ctx, "ws.pvol", npores);

@@ -54,3 +54,9 @@ def load_example(golden_dir):
     shape = tuple(int(v) for v in z["shape"])
     n = int(np.prod(shape))
     return np.unpackbits(z["bits"])[:n].reshape(shape).astype(np.uint8)
+
+
+def large_case():
+    """2^24 voxels (256^3): the size from which plateaus are labelled by pointer jumping and
+    unions of recorded parent pairs. A union of 6000 spheres, radii U[4, 12]."""
+    return synth.sphere_union((256, 256, 256), count=6000, rmin=4.0, rmax=12.0, seed=77)

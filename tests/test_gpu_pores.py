@@ -126,3 +126,28 @@ def test_watershed_with_most_voxels_shared(ctx, oracle_mod):
     pws, tws = g["ws_table"]
     assert pws == r.pores_ws and tws == r.throats_ws
     assert len(tws) > 0
+
+
+def test_pores_and_watershed_large_volume_matches_oracle_fixture(ctx):
+    """2^24 voxels, where the plateaus are labelled by pointer jumping and unions of recorded
+    parent pairs: pores, shared voxels and the whole watershed against the oracle's results
+    (tests/golden/large_case.json.gz, made by tests/golden/make_large_case.py; the oracle takes
+    minutes at this size)."""
+    import gzip
+    import json
+    import os
+    from cases import large_case
+    from util import canonical_throats
+    with gzip.open(os.path.join(GOLDEN, "large_case.json.gz"), "rt") as f:
+        rec = json.load(f)
+    vol = large_case()
+    assert list(vol.shape) == rec["shape"] and digest(vol) == rec["solid_digest"]
+    g = _gpu_pipeline(ctx, vol, False)
+    p0, t0 = g["initial"]
+    assert p0 == rows(rec["pores0"])
+    assert sorted([t[2], t[1]] for t in t0) == [[a, b] for a, b in rows(rec["throats0_lists"])]
+    assert digest(canonical_throats(g["labels_initial"])) == rec["labels_initial_canonical"]
+    assert g["table"][0] == rows(rec["pores"])
+    assert digest(canonical_throats(g["labels"])) == rec["labels_canonical"]
+    assert digest(g["ws"]) == rec["labels_ws"]
+    assert g["ws_table"] == (rows(rec["pores_ws"]), rows(rec["throats_ws"]))

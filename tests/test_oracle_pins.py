@@ -112,3 +112,17 @@ def test_shipped_coordinates_are_valid_winners(oracle_mod):
     lex_m = (mine[0] * 10000 + mine[1]) * 10000 + mine[2]
     lex_t = (theirs[0] * 10000 + theirs[1]) * 10000 + theirs[2]
     assert (lex_m < lex_t).all()
+
+
+def test_large_case_volume_matches_its_fixture():
+    """The 2^24-voxel parity volume rebuilt here is the one the fixture was made from."""
+    import gzip
+    import hashlib
+    import json
+    import os
+    from cases import large_case
+    with gzip.open(os.path.join(os.path.dirname(__file__), "golden", "large_case.json.gz"), "rt") as f:
+        rec = json.load(f)
+    vol = large_case()
+    assert list(vol.shape) == rec["shape"]
+    assert hashlib.sha256(np.ascontiguousarray(vol).tobytes()).hexdigest() == rec["solid_digest"]
