@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "devutil.cuh"
+#include "ordered_sort.h"
 
 namespace pma {
 namespace {
@@ -1071,10 +1072,11 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemcpyAsync(h_r2.data(), ball_r2, nb * 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
     }
-    // std::sort with the reference's comparator (PoreAndThroatComputer.cpp:121-122), run on a
-    // host thread while the plateau kernels below run. The items are 8-byte (r2, scan index)
-    // pairs compared on r2 alone: std::sort's moves depend only on comparison results, so
-    // the permutation equals the one the reference's 16-byte balls go through.
+    // std::sort with the reference's comparator (PoreAndThroatComputer.cpp:121-122), run on
+    // host threads (ordered_sort: the same permutation) while the plateau kernels below run.
+    // The items are 8-byte (r2, scan index) pairs compared on r2 alone: std::sort's moves
+    // depend only on comparison results, so the permutation equals the one the reference's
+    // 16-byte balls go through.
     std::vector<unsigned long long> items(nb);
     for (int64_t i = 0; i < nb; ++i)
         items[i] = (static_cast<unsigned long long>(h_r2[i]) << 32) | static_cast<unsigned long long>(i);
@@ -1085,8 +1087,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         }
     } sorter;
     sorter.t = std::thread([&items] {
-        std::sort(items.begin(), items.end(),
-                  [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); });
+        ordered_sort(items.begin(), items.end(),
+                     [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); });
     });
 
     // Plateaus: connected sets of equal crad under the stencil.
