@@ -62,8 +62,6 @@ struct WsState {
     uint32_t ext_cap;
     unsigned int* pbound;         // per pore
     unsigned int* err;
-    uint32_t* slot_gen;           // generation stamp of same-depth claims, per event slot
-    uint32_t* slot_voxel;
     uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
     unsigned int* bfill;
@@ -245,24 +243,20 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
 }
 
 // Ordered compaction of a generation's same-depth claims into the next frontier, in event
-// order. Two forms:
-//  * small generations (up to kLookbackChunks chunks of kChunk events) compact inside the
-//    resolve phase: each chunk (one block, four events per thread) ranks its claims, and its
-//    offset comes from a decoupled look-back over the chunks before it, read 32 descriptors at
-//    a time by one warp. A descriptor holds (generation << 40) | state << 38 | count, state
-//    1 = the chunk's own count, 2 = the inclusive prefix; one of an older generation is not
-//    yet published. Chunks publish their own count before looking back and every block of
-//    the cooperative grid is resident, so the look-back always ends; it is bounded all the
-//    same (err bit 16). This saves two of the four grid-wide barriers of a generation.
-//  * larger ones stamp their claims into event slots (generation number and voxel), count
-//    them per chunk, and compact in two more phases: an exclusive scan of the chunk counts
-//    (block 0) and the scatter of the stamped slots.
-// (The look-back alone serialises the chunks of a large generation: 907 -> 1108 ms per
-// 1024^3 step when every generation used it.)
+// order, inside the resolve phase: each chunk of kChunk events (one block, four per thread)
+// ranks its claims, and its offset comes from a decoupled look-back over the chunks before it,
+// read 32 descriptors at a time by one warp. A descriptor holds (generation << 40) | state << 38
+// | count, state 1 = the chunk's own count, 2 = the inclusive prefix; one of an older
+// generation is not yet published. Chunks publish their own count before looking back and
+// every block of the cooperative grid is resident, so the look-back always ends; it is bounded
+// all the same (err bit 16). A generation thus needs two grid-wide barriers (after the claims,
+// after the resolved frontier) instead of four for a separate count, scan and scatter.
+// (Measured at 1024^3: 894 ms per step, against 910-950 ms with the count / scan / scatter
+// form for generations of more than 256 chunks, and 1108 ms with a look-back that read one
+// descriptor at a time.)
 constexpr unsigned long long kDescOwn = 1ull << 38;
 constexpr unsigned long long kDescIncl = 2ull << 38;
 constexpr unsigned long long kDescVal = (1ull << 38) - 1;
-constexpr unsigned long long kLookbackChunks = 256;
 
 // Called by all 32 lanes of one warp; returns the exclusive prefix of chunk c.
 __device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned long long c, unsigned long long gen,
@@ -303,95 +297,17 @@ __device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned lon
     return excl;
 }
 
-__device__ __forceinline__ void ws_slot_scan(unsigned int* ccount, unsigned long long nev, unsigned int* ng_next,
-                                             unsigned int* part) {
-    const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
-    const unsigned long long per = (nchunks + blockDim.x - 1) / blockDim.x;
-    unsigned int sum = 0;
-    for (unsigned long long k = 0; k < per; ++k) {
-        const unsigned long long c = threadIdx.x * per + k;
-        if (c < nchunks) sum += __ldcg(ccount + c);
-    }
-    part[threadIdx.x] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned int run = 0;
-        for (unsigned t = 0; t < blockDim.x; ++t) {
-            const unsigned int v = part[t];
-            part[t] = run;
-            run += v;
-        }
-        *ng_next = run;
-    }
-    __syncthreads();
-    unsigned int run = part[threadIdx.x];
-    for (unsigned long long k = 0; k < per; ++k) {
-        const unsigned long long c = threadIdx.x * per + k;
-        if (c < nchunks) {
-            const unsigned int v = __ldcg(ccount + c);
-            ccount[c] = run;
-            run += v;
-        }
-    }
-}
-
-// blockDim.x == kChunk / 4: each thread owns 4 consecutive slots of the block's chunk.
-__device__ __forceinline__ void ws_slot_scatter(const uint32_t* slot_gen, const uint32_t* slot_voxel,
-                                                unsigned long long nev, uint32_t gen, const unsigned int* coff,
-                                                const uint32_t* gp, uint32_t* nv, uint32_t* np_,
-                                                unsigned int* warp_sum) {
-    const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const unsigned int base = __ldcg(coff + c);
-        const unsigned long long e0 = c * kChunk + static_cast<unsigned long long>(threadIdx.x) * 4;
-        unsigned int f[4];
-        unsigned int mine = 0;
-        for (int k = 0; k < 4; ++k) {
-            const unsigned long long e = e0 + k;
-            f[k] = (e < nev && __ldcg(slot_gen + e) == gen) ? 1u : 0u;
-            mine += f[k];
-        }
-        unsigned int incl = mine;
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= static_cast<unsigned>(o)) incl += t;
-        }
-        if (lane == 31) warp_sum[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            const unsigned nw = blockDim.x / 32;
-            unsigned int wsum = lane < nw ? warp_sum[lane] : 0u;
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned int t = __shfl_up_sync(0xFFFFFFFFu, wsum, o);
-                if (lane >= static_cast<unsigned>(o)) wsum += t;
-            }
-            if (lane < nw) warp_sum[lane] = wsum;  // inclusive over warps
-        }
-        __syncthreads();
-        unsigned int pos = base + (warp ? warp_sum[warp - 1] : 0u) + incl - mine;
-        for (int k = 0; k < 4; ++k) {
-            if (!f[k]) continue;
-            const unsigned long long e = e0 + k;
-            nv[pos] = __ldcg(slot_voxel + e);
-            np_[pos] = __ldcg(gp + e / 27);
-            ++pos;
-        }
-        __syncthreads();
-    }
-}
-
-// Up to max_gens generations of one depth in a single cooperative launch, with grid-wide
-// barriers between the phases. ng[2] holds the two frontier sizes; the frontier starts on
-// side `cur`. out[0] = generations run, out[1] = the side holding the next frontier.
+// Up to max_gens generations of one depth in a single cooperative launch, two grid-wide
+// barriers per generation. ng[2] holds the two frontier sizes; the frontier starts on side
+// `cur`. out[0] = generations run, out[1] = the side holding the next frontier.
 __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint32_t* gv0, uint32_t* gp0, uint32_t* gv1,
-                                                             uint32_t* gp1, unsigned int* ng, unsigned int* ccount,
+                                                             uint32_t* gp1, unsigned int* ng,
                                                              unsigned long long* desc, uint32_t depth,
                                                              unsigned long long gen0, int max_gens, int cur,
                                                              unsigned long long* out) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
-    __shared__ unsigned int part[kChunk / 4];
+    __shared__ unsigned int part[33];
     const unsigned long long tid = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
     const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, lt = (1u << lane) - 1u;
@@ -411,7 +327,6 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
         // Resolve by chunks of kChunk events: event k * blockDim + t of a chunk is thread t's
         // k-th, so event order is k-major, then thread.
         const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
-        const bool fused = nchunks <= kLookbackChunks;  // the same for every block
         for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
             bool f[4];
             uint32_t wv[4], wp[4];
@@ -420,10 +335,6 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
             for (int k = 0; k < 4; ++k) {
                 const unsigned long long seq = c * kChunk + k * (kChunk / 4) + threadIdx.x;
                 f[k] = seq < nev && ws_resolve_event(s, gv, gp, seq, depth, gen, wv[k], wp[k]);
-                if (!fused && f[k]) {
-                    s.slot_voxel[seq] = wv[k];
-                    s.slot_gen[seq] = static_cast<uint32_t>(gen);
-                }
                 m[k] = __ballot_sync(0xFFFFFFFFu, f[k]);
                 if (lane == 0) part[k * (kChunk / 128) + warp] = __popc(m[k]);
             }
@@ -436,37 +347,25 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
                     if (lane >= static_cast<unsigned>(o)) incl += t2;
                 }
                 const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-                if (fused) {
-                    part[lane] = incl - v;
-                    const unsigned long long base = ws_lookback(desc, c, gen, total, s.err, lane);
-                    if (lane == 0) {
-                        part[32] = static_cast<unsigned int>(base);
-                        if (c == nchunks - 1) ng[cur ^ 1] = static_cast<unsigned int>(base + total);
-                    }
-                } else if (lane == 0) {
-                    ccount[c] = total;
+                part[lane] = incl - v;
+                const unsigned long long base = ws_lookback(desc, c, gen, total, s.err, lane);
+                if (lane == 0) {
+                    part[32] = static_cast<unsigned int>(base);
+                    if (c == nchunks - 1) ng[cur ^ 1] = static_cast<unsigned int>(base + total);
                 }
             }
             __syncthreads();
-            if (fused) {
-                const unsigned base = part[32];
+            const unsigned base = part[32];
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (f[k]) {
-                        const unsigned pos = base + part[k * (kChunk / 128) + warp] + __popc(m[k] & lt);
-                        nv[pos] = wv[k];
-                        np_[pos] = wp[k];
-                    }
-                __syncthreads();  // part is reused by the next chunk
-            }
+            for (int k = 0; k < 4; ++k)
+                if (f[k]) {
+                    const unsigned pos = base + part[k * (kChunk / 128) + warp] + __popc(m[k] & lt);
+                    nv[pos] = wv[k];
+                    np_[pos] = wp[k];
+                }
+            __syncthreads();  // part is reused by the next chunk
         }
         grid.sync();
-        if (!fused) {
-            if (blockIdx.x == 0) ws_slot_scan(ccount, nev, ng + (cur ^ 1), part);
-            grid.sync();
-            ws_slot_scatter(s.slot_gen, s.slot_voxel, nev, static_cast<uint32_t>(gen), ccount, gp, nv, np_, part);
-            grid.sync();
-        }
         cur ^= 1;
     }
     if (tid == 0) {
@@ -778,15 +677,10 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         const size_t max_events = max_bucket * 27;
 
         ws.ev_touch = buf<uint8_t>(ctx, "ws.ev_touch", max_events);  // written for every event by phase 0
-        // frontier compaction: event slots and chunk counts (large generations), chunk
-        // descriptors (small ones); generations restart at 1 in this attempt
-        ws.slot_gen = buf<uint32_t>(ctx, "ws.slot_gen", max_events);
-        ws.slot_voxel = buf<uint32_t>(ctx, "ws.slot_voxel", max_events);
-        PMA_CUDA(cudaMemsetAsync(ws.slot_gen, 0, max_events * 4, s));
+        // chunk descriptors of the frontier compaction; generations restart at 1 in this attempt
         const size_t max_chunks = (max_events + kChunk - 1) / kChunk;
-        unsigned int* ccount = buf<unsigned int>(ctx, "ws.ccount", max_chunks);
-        auto* desc = buf<unsigned long long>(ctx, "ws.desc", std::min<size_t>(max_chunks, kLookbackChunks));
-        PMA_CUDA(cudaMemsetAsync(desc, 0, std::min<size_t>(max_chunks, kLookbackChunks) * 8, s));
+        auto* desc = buf<unsigned long long>(ctx, "ws.desc", max_chunks);
+        PMA_CUDA(cudaMemsetAsync(desc, 0, max_chunks * 8, s));
         PMA_CUDA(cudaMemcpyAsync(d_boff, boff.data(), (nb + 1) * 8ull, cudaMemcpyHostToDevice, s));
         std::vector<unsigned int> h_fill(nb, 0);
         if (npores) {
@@ -864,7 +758,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
             while (true) {
                 const uint32_t dep = static_cast<uint32_t>(depth);
                 int gens = kGensPerLaunch;
-                void* args[] = {&ws, &gvb[0], &gpb[0], &gvb[1], &gpb[1], &d_ng, &ccount, &desc,
+                void* args[] = {&ws, &gvb[0], &gpb[0], &gvb[1], &gpb[1], &d_ng, &desc,
                                 const_cast<uint32_t*>(&dep), &gen, &gens, &cur, &d_out};
                 PMA_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ws_generations), coop_grid,
                                                      kChunk / 4, args, 0, s));
