@@ -453,6 +453,10 @@ __global__ void edge_offsets(const unsigned long long* __restrict__ edges, size_
     }
 }
 
+__global__ void level_starts(const uint32_t* __restrict__ key, size_t np, uint8_t* __restrict__ flags) {
+    PMA_GRID_STRIDE(i, np) flags[i] = i == 0 || key[i] != key[i - 1];
+}
+
 __global__ void level_keys(const uint32_t* __restrict__ pcrad, size_t np, uint32_t* __restrict__ key,
                            uint32_t* __restrict__ val) {
     PMA_GRID_STRIDE(p, np) {
@@ -1135,6 +1139,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         }
     }
     ctx->check_launch("uf_hook");
+    auto kt_ids = std::make_unique<KernelTimer>(ctx, "plateau_ids");
     uf_flatten<<<G, 256, 0, s>>>(n, pid);
     ctx->check_launch("uf_flatten");
     flag_roots<<<G, 256, 0, s>>>(pid, n, flags);
@@ -1152,6 +1157,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         ctx->sync();
         PMA_REQUIRE(!(h_err & 8u), PMA_ERR_INTERNAL, "pma_pores: plateau labelling left a non-root parent");
     }
+    kt_ids.reset();
     // Edges between plateaus, sorted by destination.
     auto kt_edges = std::make_unique<KernelTimer>(ctx, "plateau_edges");
     auto* ecount = reinterpret_cast<unsigned long long*>(d_count + 1);
@@ -1223,14 +1229,18 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     uint32_t* order = buf<uint32_t>(ctx, "pores.order", np);
     std::vector<size_t> level_begin;
     if (np) {
+        KernelTimer kt(ctx, "level_order");
         level_keys<<<grid_for(ctx, np), 256, 0, s>>>(pcrad, np, lkey, lval);
         ctx->check_launch("level_keys");
         sort_pairs(ctx, lkey, lkey2, lval, order, np);
-        std::vector<uint32_t> hk(np);
-        PMA_CUDA(cudaMemcpyAsync(hk.data(), lkey2, np * 4, cudaMemcpyDeviceToHost, s));
+        // first position of each level, found on the device (a few hundred of np positions)
+        level_starts<<<grid_for(ctx, np), 256, 0, s>>>(lkey2, np, flags);
+        ctx->check_launch("level_starts");
+        const int64_t nl = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), flags, lval, np, d_count);
+        std::vector<uint32_t> starts(nl);
+        if (nl) PMA_CUDA(cudaMemcpyAsync(starts.data(), lval, nl * 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
-        for (int64_t i = 0; i < np; ++i)
-            if (i == 0 || hk[i] != hk[i - 1]) level_begin.push_back(static_cast<size_t>(i));
+        for (int64_t i = 0; i < nl; ++i) level_begin.push_back(static_cast<size_t>(starts[i]));
     }
     level_begin.push_back(static_cast<size_t>(np));
 

@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "devutil.cuh"
@@ -741,6 +742,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
             have_count = false;
             if (n0 == 0) continue;
             int cur = 0;
+            auto kt_sort = std::make_unique<KernelTimer>(ctx, "ws_depth_sort");
             if (n0 <= static_cast<size_t>(kSmallBucket)) {
                 ws_sort_small<<<1, 1024, 0, s>>>(ws.ent_time + boff[depth], ws.ent_val + boff[depth],
                                                  static_cast<unsigned>(n0), gvb[cur], gpb[cur], d_ng + cur);
@@ -753,6 +755,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
                 h_small[2] = static_cast<unsigned int>(n0);
                 PMA_CUDA(cudaMemcpyAsync(d_ng + cur, &h_small[2], 4, cudaMemcpyHostToDevice, s));
             }
+            kt_sort.reset();
             const int64_t next_depth = di + 1 < depths.size() ? depths[di + 1] : -1;
             KernelTimer kt(ctx, "ws_generations");
             while (true) {
@@ -793,6 +796,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
     PMA_REQUIRE(!(h_err & 16u), PMA_ERR_LIMIT, "pma_watershed: frontier compaction look-back did not finish");
 
+    KernelTimer kt_tables(ctx, "ws_tables");  // to the end of the stage
     // Volumes, labels and shared voxels.
     auto* pvol = buf<unsigned long long>(ctx, "ws.pvol", npores);
     uint8_t* shared_flag = buf<uint8_t>(ctx, "ws.shared_flag", n);
