@@ -635,12 +635,12 @@ __global__ void level_heavy(PlateauSets st, size_t begin) {
 
 // Sort path: every element of every predecessor set (and the own seed) of the big plateaus
 // becomes a key (plateau << shift | rank); sorting and removing duplicates yields each union.
-// Keys are 32-bit, with the plateau given by its index in the level's big list, whenever
-// ranks and big-list indices fit together; otherwise 64-bit with the level-local index.
+// The plateau of a key is its index in the level's big list, above the rank bits (32 bits
+// in the single-block merge); keys are 32-bit whenever ranks and big-list indices fit together,
+// else 64-bit, and the radix sort covers the used bits only.
 template <class K>
 __device__ __forceinline__ uint32_t key_plateau(const PlateauSets& st, K key, int shift) {
-    const uint32_t hi = static_cast<uint32_t>(key >> shift);
-    return sizeof(K) == 4 ? st.big_list[hi] : hi;
+    return st.big_list[static_cast<uint32_t>(key >> shift)];
 }
 
 // In-degrees of the big plateaus (their edges are spread over the whole grid below).
@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(256) level_expand(PlateauSets st, size_t begin
             const uint32_t q = static_cast<uint32_t>(st.edges[st.eoff[p] + (t - doff[lo])]);
             len = st.slen[q];
             src = st.pool + st.soff[q];
-            hi = static_cast<K>(sizeof(K) == 4 ? lo : L) << shift;
+            hi = static_cast<K>(lo) << shift;
         }
         // The warp's 32 sets are expanded together, 32 elements per round: element u of the
         // concatenation belongs to the last lane whose exclusive offset is <= u (a shuffle
@@ -748,7 +748,7 @@ __global__ void __launch_bounds__(256) level_expand(PlateauSets st, size_t begin
         const uint32_t p = st.order[begin + L];
         if (st.seed[p] == kNone) continue;
         const unsigned long long pos = atomicAdd(&st.info[3], 1ull);
-        if (pos < cap) keys[pos] = (static_cast<K>(sizeof(K) == 4 ? b : L) << shift) | static_cast<K>(st.seed[p]);
+        if (pos < cap) keys[pos] = (static_cast<K>(b) << shift) | static_cast<K>(st.seed[p]);
     }
 }
 
@@ -782,7 +782,7 @@ __global__ void __launch_bounds__(1024) level_merge_small(PlateauSets st, size_t
         const uint32_t L = st.big_list[b];
         const uint32_t p = st.order[begin + L];
         const unsigned e0 = st.eoff[p], e1 = st.eoff[p + 1];
-        const unsigned long long hi = static_cast<unsigned long long>(L) << 32;
+        const unsigned long long hi = static_cast<unsigned long long>(b) << 32;
         for (unsigned e = e0 + lane; e < e1; e += 32) {
             const uint32_t q = static_cast<uint32_t>(st.edges[e]);
             const uint32_t len = st.slen[q];
@@ -845,10 +845,11 @@ __global__ void __launch_bounds__(1024) level_merge_small(PlateauSets st, size_t
     for (unsigned t = 0; t < per; ++t) {
         const unsigned i = i0 + t;
         if (!(i < n && (i == 0 || sk[i - 1] != sk[i]))) continue;
-        const uint32_t L = static_cast<uint32_t>(sk[i] >> 32);
+        const uint32_t bhi = static_cast<uint32_t>(sk[i] >> 32);  // index in the big list
+        const uint32_t L = st.big_list[bhi];
         keys[u] = sk[i];
         // sk[i] is a first copy, so sk[i - 1] is the previous distinct key
-        if (i == 0 || static_cast<uint32_t>(sk[i - 1] >> 32) != L) st.first[L] = u;
+        if (i == 0 || static_cast<uint32_t>(sk[i - 1] >> 32) != bhi) st.first[L] = u;
         atomicAdd(&st.cnt[L], 1ull);
         ++u;
     }
@@ -891,9 +892,12 @@ __global__ void level_copy_big(const K* __restrict__ keys, size_t n_host, Platea
     const size_t n = n_dev ? static_cast<size_t>(*n_dev) : n_host;
     PMA_GRID_STRIDE(i, n) {
         const uint32_t L = key_plateau(st, keys[i], shift);
-        const unsigned long long pos = b0 + st.off[L];
-        if (pos + st.cnt[L] <= st.pool_cap)
-            st.pool[pos + (i - st.first[L])] = static_cast<uint32_t>(keys[i] & low);
+        const unsigned long long pos = b0 + st.off[L], r = i - st.first[L];  // rank within the set
+        if (r >= st.cnt[L]) {  // keys and set bounds disagree: never write outside the set
+            atomicOr(st.err, 32u);
+            continue;
+        }
+        if (pos + st.cnt[L] <= st.pool_cap) st.pool[pos + r] = static_cast<uint32_t>(keys[i] & low);
     }
 }
 
@@ -1346,6 +1350,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                         ctx->check_launch("level_runs");
                     }
                 } else {
+                    shift = rank_bits;
                     auto* k64 = buf<unsigned long long>(ctx, "pores.lkeys", total);
                     auto* k64b = buf<unsigned long long>(ctx, "pores.lkeys2", total);
                     int64_t emitted = 0;
@@ -1355,8 +1360,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                         ctx->check_launch("level_expand");
                         emitted = read_emitted();
                     }
-                    int bits = 32;
-                    while (bits < 64 && (1ull << (bits - 32)) < e - b) ++bits;
+                    const int bits = rank_bits + big_bits;  // radix passes over the used bits only
                     {
                         KernelTimer kt3(ctx, "merge_sort");
                         sort_keys(ctx, k64, k64b, emitted, bits);
@@ -1392,6 +1396,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemcpyAsync(&used, base, 8, cudaMemcpyDeviceToHost, s));
         ctx->sync();
         PMA_REQUIRE(!(h_err & 1u), PMA_ERR_LIMIT, "pma_pores: plateau union-find did not converge");
+        PMA_REQUIRE(!(h_err & 32u), PMA_ERR_INTERNAL, "pma_pores: merged seed sets disagree with their bounds");
         if (!(h_err & 2u)) break;
         PMA_REQUIRE(attempt < 2, PMA_ERR_MEMORY, "pma_pores: seed-set pool overflow");
         pool_cap = used + (used >> 2) + 1024;
