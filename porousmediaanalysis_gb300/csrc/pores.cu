@@ -13,10 +13,12 @@
 //    earlier seed, which then reaches all it reaches). With m(p) the smallest rank of a ball
 //    reaching plateau p, p's smallest-rank ball is a seed iff it beats m of every plateau
 //    with an edge into p.
-//  * Both recurrences run plateau by plateau in decreasing crad, a pair of launches per
-//    crad level. The ball order comes from std::sort on the host applied to the same
-//    sequence (z, x, y scan order) with the same comparator, so equal radii tie-break
-//    exactly as in the reference.
+//  * Plateaus are found by a union-find over equal-crad neighbours (from 2^24 voxels:
+//    pointer jumping on the initial trees, then unions of the recorded parent pairs).
+//  * Both recurrences run plateau by plateau in decreasing crad, a few launches per crad
+//    level. The ball order is std::sort's on the host (ordered_sort: libstdc++'s own
+//    introsort steps on several threads) applied to the same sequence (z, x, y scan order)
+//    with the same comparator, so equal radii tie-break exactly as in the reference.
 //  * A voxel's label is its seed's pore id when |S| = 1 and a shared type ("throat") when
 //    |S| >= 2. Pore volumes, boundary flags, type volumes and type pore lists are exact.
 //    The reference numbers types in its depth-first creation order, which also consumed ids
