@@ -4,7 +4,7 @@ One step = the full pipeline over one synthetic volume: EDT -> containing balls 
 pore propagation -> empty-pore removal -> watershed, plus float64 geodesics
 (EuclideanDistanceComputer .. WatershedComputer and ShortestPathComputer of the reference).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload spinodal1024|grf512|grf320|union128]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload spinodal1024|spinodal384|grf512|grf320|union128]
   python bench.py --serve [--serve-requests R]   the serving loop (its own JSON line)
   python bench.py --impl reference ...           the CPU restatement (oracle) on bounded samples
 
