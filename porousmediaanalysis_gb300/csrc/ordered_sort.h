@@ -14,6 +14,7 @@
 #pragma once
 
 #include <algorithm>
+#include <system_error>
 #include <thread>
 
 namespace pma {
@@ -35,9 +36,14 @@ void ordered_sort_rec(It first, It last, long depth, Comp comp, int levels) {
     }
     --depth;
     It cut = std::__unguarded_partition_pivot(first, last, comp);
-    std::thread right([=] { ordered_sort_rec(cut, last, depth, comp, levels - 1); });
+    std::thread right;
+    try {
+        right = std::thread([=] { ordered_sort_rec(cut, last, depth, comp, levels - 1); });
+    } catch (const std::system_error&) {  // no thread to be had: the same steps, in line
+        ordered_sort_rec(cut, last, depth, comp, 0);
+    }
     ordered_sort_rec(first, cut, depth, comp, levels - 1);
-    right.join();
+    if (right.joinable()) right.join();
 }
 
 }  // namespace detail
