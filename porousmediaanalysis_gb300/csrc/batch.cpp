@@ -12,6 +12,7 @@
 #include <atomic>
 #include <numeric>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -89,7 +90,13 @@ extern "C" int pma_pipeline_batch(pma_ctx* ctx, pma_batch_item* items, size_t n,
             }
         };
         std::vector<std::thread> threads;
-        for (size_t l = 1; l < want; ++l) threads.emplace_back(work, ctx->lanes[l]);
+        for (size_t l = 1; l < want; ++l) {
+            try {
+                threads.emplace_back(work, ctx->lanes[l]);
+            } catch (const std::system_error&) {
+                break;  // fewer host threads: the lanes that run take the remaining volumes
+            }
+        }
         work(ctx->lanes[0]);
         for (std::thread& t : threads) t.join();
         for (size_t i = 0; i < n; ++i)

@@ -196,7 +196,20 @@ int pma_server_create(pma_ctx* ctx, const pma_server_config* cfg, pma_server** o
             delete s;
             throw;
         }
-        for (size_t i = 0; i < s->lanes.size(); ++i) s->lanes[i].thread = std::thread(pma::lane_loop, s, i);
+        try {
+            for (size_t i = 0; i < s->lanes.size(); ++i) s->lanes[i].thread = std::thread(pma::lane_loop, s, i);
+        } catch (...) {  // stop the lanes already started before giving the server up
+            {
+                std::lock_guard<std::mutex> lock(s->mu);
+                s->stopping = true;
+                s->cv_work.notify_all();
+            }
+            for (pma_server::Lane& l : s->lanes)
+                if (l.thread.joinable()) l.thread.join();
+            for (pma_server::Lane& l : s->lanes) pma_ctx_destroy(l.ctx);
+            delete s;
+            throw pma::Error(PMA_ERR_CUDA, "pma_server_create: could not start the lane threads");
+        }
         *out = s;
     });
 }
