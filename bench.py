@@ -43,10 +43,10 @@ WORKLOADS = {
 }
 
 # DRAM bytes per voxel measured by ncu over all launches of a kernel in one step of a 320^3
-# GRF (profiles/), used as the roofline's `traffic` when that kernel dominates.
+# GRF, used as the roofline's `traffic` when that kernel dominates.
 TRAFFIC_PER_VOXEL = {
     "ws_generations": (268.0, "ncu dram__bytes_read+write of all ws_generations launches of one 320^3 "
-                              "GRF step (profiles/launches_grf320_pipeline.md), scaled by voxels"),
+                              "GRF step, scaled by voxels"),
 }
 
 # Algorithmic HBM bytes per voxel of the timed kernels (reads + writes each kernel must do).

@@ -65,6 +65,24 @@ uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
  * pass a buffer large enough for the whole report. Returns its full length. */
 int pma_ctx_set_timing(pma_ctx* ctx, int enable);
 size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap);
+/* Bounds of the data-dependent device loops. Each loop that reaches its bound stops and the
+ * call returns PMA_ERR_LIMIT, with the context still usable. No counterpart in the
+ * reference, whose loops run on the host; the defaults are far above what any volume of
+ * fewer than 2^32 voxels needs. Batch lanes and server lanes created later inherit them. */
+typedef struct pma_limits {
+    int32_t spin_limit;             /* polls of one device-side wait on another block (2^20) */
+    int32_t union_limit;            /* link attempts of one plateau union in the union-find (2^22) */
+    uint64_t watershed_generations; /* FIFO generations of one watershed call (2^23 - 1) */
+    uint64_t geodesic_buckets;      /* distance buckets of one cavity's flood (0: 2 * voxels + 64) */
+} pma_limits;
+int pma_ctx_get_limits(const pma_ctx* ctx, pma_limits* out);
+int pma_ctx_set_limits(pma_ctx* ctx, const pma_limits* limits);
+/* Runs one bounded device wait on a flag that nothing sets (the watershed's frontier
+ * look-back waiting for a chunk that never publishes), with the context's spin_limit. Sets
+ * *timed_out = 1 when the wait gave up and reported it, as it must. No counterpart in the
+ * reference; it exercises the error path of the device waits without faulting anything. */
+int pma_selftest_bounded_wait(pma_ctx* ctx, int* timed_out);
+
 /* Device bytes held by ctx's scratch cache and its memory pool (freed blocks are kept for
    reuse), batch lanes included; pma_ctx_trim releases them. */
 size_t pma_ctx_scratch_bytes(const pma_ctx* ctx);
@@ -177,7 +195,11 @@ typedef struct pma_cavity {     /* a row of cavityDescriptions.txt (Serializer.c
  * ids. Replaces ShortestPathComputer::ComputeShortestPathDistances
  * (ShortestPathComputer.cpp:39-511). Distances: -1 solid, FLT_MAX (DBL_MAX) unreached;
  * cavity ids: 0 solid, UINT32_MAX unreached. The f32 variant is bit-exact with the
- * reference; the f64 variant accumulates the same steps in double precision. */
+ * reference; the f64 variant accumulates the same steps in double precision.
+ * Cavity rows (cavityDescriptions.txt, ShortestPathComputer.cpp:143-164): the first
+ * cavity_cap rows are written to h_cavities and *n_cavities receives the number of
+ * cavities, which may exceed cavity_cap (call again with a larger buffer to get them all;
+ * cavity_cap 0 with h_cavities NULL only counts). */
 int pma_geodesic_f32(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_stencil stencil,
                      float* d_dist, uint32_t* d_cavity, pma_cavity* h_cavities, int cavity_cap,
                      int* n_cavities);
@@ -205,9 +227,10 @@ typedef struct pma_outputs {
     uint64_t maximum_balls_count;
     pma_table* pores;           /* after empty-pore removal (caller frees) */
     pma_table* watershed;       /* watershed pores and throats (caller frees) */
-    pma_cavity cavities[16];
-    int n_cavities;
-    int pad_;
+    pma_cavity cavities[16];    /* the first 16 cavity rows */
+    int n_cavities;             /* the number of cavities (may exceed 16) */
+    int cavity_rows_cap;        /* capacity of cavity_rows */
+    pma_cavity* cavity_rows;    /* optional host buffer: receives the first cavity_rows_cap rows */
 } pma_outputs;
 
 typedef struct pma_options {

@@ -1,9 +1,10 @@
 #!/bin/sh
 # Compiles the reference's own C++ sources (where they lie, read-only) into the checker
 # binary oracle/_ref/pma_ref, with oracle/ref_shim standing in for FreeImage. Test
-# infrastructure only; needs the reference tree (default /root/reference).
+# infrastructure only; needs the reference tree: the first argument, else $PMA_REFERENCE_DIR,
+# else /root/reference.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${PMA_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 mkdir -p "$OUT/obj"

@@ -73,6 +73,8 @@ def lib():
         l.orc_table_pool.restype = ctypes.POINTER(ctypes.c_uint32)
         l.orc_table_free.argtypes = [P]
         l.orc_table_free.restype = None
+        l.orc_table_from_pores.argtypes = [P, ctypes.c_size_t]
+        l.orc_table_from_pores.restype = P
         for fn in (l.orc_geodesic_f32, l.orc_geodesic_f64):
             fn.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P,
                            ctypes.c_int]
@@ -177,16 +179,37 @@ def pores_and_watershed(mask, edt2, crad2, max_edt2, d3q7=False):
     return r
 
 
+def watershed(pore_rows, crad2, max_edt2, d3q7=False):
+    """a12 alone: the watershed from pores given as rows (id, x, y, z, r2, boundary, volume).
+    Returns (labels_ws, pores_ws, throats_ws)."""
+    l = lib()
+    crad2 = np.ascontiguousarray(crad2, dtype=np.uint32)
+    sx, sy, sz = _dims(crad2)
+    arr = (_Pore * max(1, len(pore_rows)))(*[_Pore(*p) for p in pore_rows])
+    h = l.orc_table_from_pores(arr, len(pore_rows))
+    ws = np.zeros(crad2.shape, dtype=np.uint32)
+    h2 = l.orc_watershed(h, _p(crad2), sx, sy, sz, int(d3q7), max_edt2, _p(ws))
+    pores, throats = _table(h2)
+    l.orc_table_free(h)
+    l.orc_table_free(h2)
+    return ws, pores, throats
+
+
 def geodesic(solid, d3q7=False, fp64=False):
     """(dist float32/float64, cavity uint32, cavity rows)."""
     solid = np.ascontiguousarray(solid, dtype=np.uint8)
     sx, sy, sz = _dims(solid)
     dist = np.empty(solid.shape, dtype=np.float64 if fp64 else np.float32)
     cav = np.empty(solid.shape, dtype=np.uint32)
-    rows = (_Cavity * 64)()
     fn = lib().orc_geodesic_f64 if fp64 else lib().orc_geodesic_f32
-    n = fn(_p(solid), sx, sy, sz, int(d3q7), _p(dist), _p(cav), rows, 64)
-    assert n >= 0
+    cap = 64
+    while True:  # the call returns the number of cavities; rerun with room for all of them
+        rows = (_Cavity * cap)()
+        n = fn(_p(solid), sx, sy, sz, int(d3q7), _p(dist), _p(cav), rows, cap)
+        assert n >= 0
+        if n <= cap:
+            break
+        cap = n
     out = [(c.id, c.seed_x, c.seed_y, c.seed_z, c.distance_to_center, c.void_count,
             c.reached_walls, c.reaches_all_walls) for c in rows[:n]]
     return dist, cav, out

@@ -527,6 +527,14 @@ extern "C" orc_table* orc_watershed(const orc_table* pores_after_removal, const 
     return make_table(st.pores, st.throats);
 }
 
+// A pores table from rows (a pores.txt read back, Serializer.cpp:104-128), for watershed runs
+// on hand-made seeds.
+extern "C" orc_table* orc_table_from_pores(const orc_pore* pores, size_t n) {
+    orc_table* t = new orc_table;
+    t->pores.assign(pores, pores + n);
+    return t;
+}
+
 extern "C" size_t orc_table_npores(const orc_table* t) { return t->pores.size(); }
 extern "C" const orc_pore* orc_table_pores(const orc_table* t) { return t->pores.data(); }
 extern "C" size_t orc_table_nthroats(const orc_table* t) { return t->throats.size(); }
@@ -690,7 +698,7 @@ struct Geodesic {
             walls_reached.clear();
             cavity_id += 127;
             dijkstra(start, cavity_id);
-            if (ncav < cav_cap) {  // SPC.cpp:143-164
+            if (ncav < cav_cap && cav) {  // SPC.cpp:143-164 (every cavity is counted)
                 orc_cavity& o = cav[ncav];
                 std::memset(&o, 0, sizeof(o));
                 o.id = cavity_id;
@@ -708,7 +716,7 @@ struct Geodesic {
             previous = processed;
             if (static_cast<int>(walls_reached.size()) == walls) break;
         }
-        return std::min(ncav, cav_cap);
+        return ncav;  // the number of cavities; rows beyond cav_cap are not stored
     }
 };
 

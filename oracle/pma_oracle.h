@@ -93,10 +93,11 @@ const orc_throat* orc_table_throats(const orc_table* t);
 size_t orc_table_pool_size(const orc_table* t);
 const uint32_t* orc_table_pool(const orc_table* t);
 void orc_table_free(orc_table* t);
+orc_table* orc_table_from_pores(const orc_pore* pores, size_t n);
 
 /* a13-a15: geodesic distances, cavity ids and cavity descriptions
- * (ShortestPathComputer.cpp:39-511). Returns the number of cavities written (<= cav_cap),
- * or -1 on error. The f64 variant is the FP64 restatement of the same algorithm. */
+ * (ShortestPathComputer.cpp:39-511). Returns the number of cavities (the first cav_cap of
+ * them are written to cav), or -1 on error. The f64 variant is the FP64 restatement of the same algorithm. */
 int orc_geodesic_f32(const uint8_t* solid, int sx, int sy, int sz, int d3q7,
                      float* dist, uint32_t* cavity, orc_cavity* cav, int cav_cap);
 int orc_geodesic_f64(const uint8_t* solid, int sx, int sy, int sz, int d3q7,

@@ -75,6 +75,28 @@ class Context:
     def set_timing(self, enable=True):
         capi.check(capi.lib().pma_ctx_set_timing(self.handle, int(enable)))
 
+    @property
+    def limits(self):
+        """Bounds of the device loops: dict of spin_limit, union_limit,
+        watershed_generations and geodesic_buckets (pma_limits)."""
+        lim = capi.Limits()
+        capi.check(capi.lib().pma_ctx_get_limits(self.handle, ctypes.byref(lim)))
+        return {name: getattr(lim, name) for name, _ in capi.Limits._fields_}
+
+    def set_limits(self, **kw):
+        """Changes some of the loop bounds (others keep their values)."""
+        cur = self.limits
+        cur.update(kw)
+        lim = capi.Limits(**cur)
+        capi.check(capi.lib().pma_ctx_set_limits(self.handle, ctypes.byref(lim)))
+
+    def selftest_bounded_wait(self):
+        """True when a device wait on a flag nothing sets gave up after spin_limit polls and
+        reported it (pma_selftest_bounded_wait)."""
+        t = ctypes.c_int()
+        capi.check(capi.lib().pma_selftest_bounded_wait(self.handle, ctypes.byref(t)))
+        return bool(t.value)
+
     def timing_report(self):
         """{kernel: (total_ms, launches)} of timed kernels since the previous report."""
         import json
@@ -182,25 +204,44 @@ def assign_watershed_ids(ctx, table, crad2, max_edt2, stencil=D3Q27):
     return labels, Table(h)
 
 
-def compute_shortest_path_distances(ctx, solid, stencil=D3Q27, fp64=False):
-    """Returns (dist float32/float64 tensor, cavity int32 tensor, cavity rows)."""
+def compute_shortest_path_distances(ctx, solid, stencil=D3Q27, fp64=False, cavity_cap=None):
+    """Returns (dist float32/float64 tensor, cavity int32 tensor, cavity rows). Every cavity's
+    row is returned; with cavity_cap given, at most that many rows are kept (the rest are
+    counted: see shortest_path_with_count)."""
+    if cavity_cap is not None:
+        return _shortest_path(ctx, solid, stencil, fp64, cavity_cap)[:3]
+    dist, cav, out, n = _shortest_path(ctx, solid, stencil, fp64, 64)
+    if n > 64:  # more cavities than the first buffer held: run again with room for all
+        dist, cav, out, n = _shortest_path(ctx, solid, stencil, fp64, n)
+    return dist, cav, out
+
+
+def shortest_path_with_count(ctx, solid, stencil=D3Q27, fp64=False, cavity_cap=64):
+    """(dist, cavity, the first cavity_cap rows, the number of cavities)."""
+    return _shortest_path(ctx, solid, stencil, fp64, cavity_cap)
+
+
+def _shortest_path(ctx, solid, stencil, fp64, cavity_cap):
     import torch
     dist = torch.empty(solid.shape, dtype=torch.float64 if fp64 else torch.float32,
                        device=solid.device)
     cav = torch.empty(solid.shape, dtype=torch.int32, device=solid.device)
-    rows = (capi.Cavity * 64)()
+    cap = cavity_cap
+    rows = (capi.Cavity * cap)()
     n = ctypes.c_int()
     fn = capi.lib().pma_geodesic_f64 if fp64 else capi.lib().pma_geodesic_f32
-    capi.check(fn(ctx.handle, _ptr(solid), _dims(solid), stencil, _ptr(dist), _ptr(cav), rows, 64,
+    capi.check(fn(ctx.handle, _ptr(solid), _dims(solid), stencil, _ptr(dist), _ptr(cav), rows, cap,
                   ctypes.byref(n)))
     out = [(r.id, r.seed_x, r.seed_y, r.seed_z, r.distance_to_center, r.void_count,
-            r.reached_walls, r.reaches_all_walls) for r in rows[:n.value]]
-    return dist, cav, out
+            r.reached_walls, r.reaches_all_walls) for r in rows[:min(cap, n.value)]]
+    return dist, cav, out, n.value
 
 
 def run_folder(ctx, base_folder, mode=MODE_ALL):
     capi.check(capi.lib().pma_run_folder(ctx.handle, str(base_folder).encode(), mode))
 
+
+CAVITY_ROWS = 4096  # cavity rows kept per volume by the pipeline calls
 
 _KINDS = {"edt2": "uint32", "crad2": "uint32", "cx": "uint32", "cy": "uint32", "cz": "uint32",
           "maxball_mask": "uint8", "pore_labels": "uint32", "watershed_labels": "uint32",
@@ -224,6 +265,11 @@ def _bind_outputs(out, shape, fields, given, device=None):
             res[name] = arr
         addr = arr.ctypes.data if device is None else arr.data_ptr()
         setattr(out, name, ctypes.cast(addr, type(getattr(out, name))))
+    # room for every cavity row (the call reports how many there are in n_cavities)
+    rows = (capi.Cavity * CAVITY_ROWS)()
+    res["_cavity_rows"] = rows
+    out.cavity_rows = ctypes.cast(rows, ctypes.POINTER(capi.Cavity))
+    out.cavity_rows_cap = CAVITY_ROWS
     return res
 
 
@@ -232,9 +278,12 @@ def _collect(out, res):
     res["maximum_balls_count"] = out.maximum_balls_count
     res["pores"] = Table(out.pores) if out.pores else None
     res["watershed"] = Table(out.watershed) if out.watershed else None
+    rows = res.pop("_cavity_rows")
+    if out.n_cavities > CAVITY_ROWS:
+        raise PmaError(5, "%d cavities, more rows than the %d kept" % (out.n_cavities, CAVITY_ROWS))
     res["cavities"] = [(c.id, c.seed_x, c.seed_y, c.seed_z, c.distance_to_center, c.void_count,
                         c.reached_walls, c.reaches_all_walls)
-                       for c in out.cavities[:out.n_cavities]]
+                       for c in rows[:out.n_cavities]]
     return res
 
 

@@ -57,7 +57,13 @@ class Outputs(ctypes.Structure):
                 ("dist_f64", ctypes.POINTER(ctypes.c_double)), ("cavity", c_u32p),
                 ("edt_stats", EdtStats), ("maximum_balls_count", ctypes.c_uint64),
                 ("pores", ctypes.c_void_p), ("watershed", ctypes.c_void_p),
-                ("cavities", Cavity * 16), ("n_cavities", ctypes.c_int), ("pad_", ctypes.c_int)]
+                ("cavities", Cavity * 16), ("n_cavities", ctypes.c_int), ("cavity_rows_cap", ctypes.c_int),
+                ("cavity_rows", ctypes.POINTER(Cavity))]
+
+
+class Limits(ctypes.Structure):
+    _fields_ = [("spin_limit", ctypes.c_int32), ("union_limit", ctypes.c_int32),
+                ("watershed_generations", ctypes.c_uint64), ("geodesic_buckets", ctypes.c_uint64)]
 
 
 class Options(ctypes.Structure):
@@ -94,6 +100,9 @@ _SIGNATURES = {
     "pma_ctx_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pma_ctx_timing_report": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "pma_ctx_trim": (ctypes.c_int, [ctypes.c_void_p]),
+    "pma_ctx_get_limits": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Limits)]),
+    "pma_ctx_set_limits": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Limits)]),
+    "pma_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "pma_edt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_void_p,
                                ctypes.POINTER(EdtStats), ctypes.c_void_p, ctypes.c_size_t]),
     "pma_pipeline_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_size_t,

@@ -29,6 +29,7 @@ pma_ctx* make_lane(const pma_ctx* parent) {
     c->num_sms = parent->num_sms;
     c->smem_optin = parent->smem_optin;
     c->timing = false;
+    c->limits = parent->limits;
     const cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;

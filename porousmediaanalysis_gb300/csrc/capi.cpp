@@ -185,6 +185,32 @@ uint64_t pma_ctx_launch_count(const pma_ctx* ctx) {
     return total;
 }
 
+int pma_ctx_get_limits(const pma_ctx* ctx, pma_limits* out) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx && out, PMA_ERR_ARGUMENT, "pma_ctx_get_limits: null argument");
+        *out = ctx->limits;
+    });
+}
+
+int pma_ctx_set_limits(pma_ctx* ctx, const pma_limits* limits) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx && limits, PMA_ERR_ARGUMENT, "pma_ctx_set_limits: null argument");
+        PMA_REQUIRE(limits->spin_limit >= 0 && limits->union_limit >= 0, PMA_ERR_ARGUMENT,
+                    "pma_ctx_set_limits: negative limit");
+        PMA_REQUIRE(limits->watershed_generations >= 1, PMA_ERR_ARGUMENT,
+                    "pma_ctx_set_limits: watershed_generations must be at least 1");
+        ctx->limits = *limits;
+    });
+}
+
+int pma_selftest_bounded_wait(pma_ctx* ctx, int* timed_out) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx && timed_out, PMA_ERR_ARGUMENT, "pma_selftest_bounded_wait: null argument");
+        PMA_CUDA(cudaSetDevice(ctx->device));
+        pma::wait_selftest(ctx, timed_out);
+    });
+}
+
 int pma_ctx_set_timing(pma_ctx* ctx, int enable) {
     return guarded([&] {
         PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
@@ -337,8 +363,9 @@ int pma_geodesic_f32(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_st
     return guarded([&] {
         PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
         PMA_CUDA(cudaSetDevice(ctx->device));
-        int n = pma::geodesic<float>(ctx, d_solid, dims, stencil, d_dist, d_cavity, h_cav, cap);
-        if (n_cav) *n_cav = n;
+        PMA_REQUIRE(cap >= 0 && (cap == 0 || h_cav), PMA_ERR_ARGUMENT, "pma_geodesic_f32: bad cavity buffer");
+        const std::vector<pma_cavity> rows = pma::geodesic<float>(ctx, d_solid, dims, stencil, d_dist, d_cavity);
+        pma::copy_cavities(rows, h_cav, cap, n_cav);
     });
 }
 
@@ -347,8 +374,9 @@ int pma_geodesic_f64(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_st
     return guarded([&] {
         PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "null context");
         PMA_CUDA(cudaSetDevice(ctx->device));
-        int n = pma::geodesic<double>(ctx, d_solid, dims, stencil, d_dist, d_cavity, h_cav, cap);
-        if (n_cav) *n_cav = n;
+        PMA_REQUIRE(cap >= 0 && (cap == 0 || h_cav), PMA_ERR_ARGUMENT, "pma_geodesic_f64: bad cavity buffer");
+        const std::vector<pma_cavity> rows = pma::geodesic<double>(ctx, d_solid, dims, stencil, d_dist, d_cavity);
+        pma::copy_cavities(rows, h_cav, cap, n_cav);
     });
 }
 

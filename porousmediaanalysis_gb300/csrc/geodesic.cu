@@ -255,8 +255,8 @@ __global__ void geo_shell_search(const uint8_t* __restrict__ solid, const T* __r
 }  // namespace
 
 template <class T>
-int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
-             uint32_t* cavity, pma_cavity* cav, int cav_cap) {
+std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
+                                 uint32_t* cavity) {
     KernelTimer kt_stage(ctx, "stage_geodesic");  // the whole stage, for the untimed remainder
     check_dims(d);
     PMA_REQUIRE(solid && dist && cavity, PMA_ERR_ARGUMENT, "pma_geodesic: null device pointer");
@@ -301,8 +301,9 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
     auto* h = static_cast<unsigned long long*>(ctx->host_staging(64));
     int half = 0;
     uint32_t cavity_id = 0;
-    int ncav = 0;
+    std::vector<pma_cavity> rows;
     const int max_buckets_per_sync = 32;
+    const uint64_t bucket_limit = ctx->limits.geodesic_buckets ? ctx->limits.geodesic_buckets : 2ull * n + 64;
     const unsigned bucket_grid = static_cast<unsigned>(ctx->num_sms * 8);
     const unsigned compact_grid = static_cast<unsigned>(std::min<size_t>(div_up(nwords, 256), ctx->num_sms * 8ull));
     while (true) {  // SPC.cpp:94-140
@@ -388,7 +389,7 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
             // after bucket k-1: lists of buckets k and k+1 hold all pending work
             if (cnt[k & 3] == 0 && cnt[(k + 1) & 3] == 0) break;
             // Distances are below 2 per voxel step, so no bucket index can exceed 2n.
-            PMA_REQUIRE(static_cast<size_t>(k) <= 2 * n + 64, PMA_ERR_LIMIT,
+            PMA_REQUIRE(static_cast<uint64_t>(k) <= bucket_limit, PMA_ERR_LIMIT,
                         "geodesic: bucket sweep did not terminate");
         }
         {
@@ -399,8 +400,8 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
         const unsigned walls_bits = static_cast<unsigned>(h[3]);
         const unsigned long long settled = h[4];
         const int reached = __builtin_popcount(walls_bits);
-        if (ncav < cav_cap && cav) {  // SPC.cpp:143-164
-            pma_cavity& o = cav[ncav];
+        {  // SPC.cpp:143-164: one row per cavity, however many there are
+            pma_cavity o;
             std::memset(&o, 0, sizeof(o));
             o.id = cavity_id;
             o.seed_x = start[0];
@@ -411,16 +412,16 @@ int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* 
             o.void_count = settled;
             const int dx = start[0] - c[0], dy = start[1] - c[1], dz = start[2] - c[2];
             o.distance_to_center = static_cast<float>(std::sqrt(static_cast<double>(dx * dx + dy * dy + dz * dz)));
+            rows.push_back(o);
         }
-        ++ncav;
         if (reached == walls_total) break;
     }
-    return std::min(ncav, cav_cap);
+    return rows;
 }
 
-template int geodesic<float>(pma_ctx*, const uint8_t*, pma_dims, pma_stencil, float*, uint32_t*,
-                             pma_cavity*, int);
-template int geodesic<double>(pma_ctx*, const uint8_t*, pma_dims, pma_stencil, double*, uint32_t*,
-                              pma_cavity*, int);
+template std::vector<pma_cavity> geodesic<float>(pma_ctx*, const uint8_t*, pma_dims, pma_stencil, float*,
+                                                 uint32_t*);
+template std::vector<pma_cavity> geodesic<double>(pma_ctx*, const uint8_t*, pma_dims, pma_stencil, double*,
+                                                  uint32_t*);
 
 }  // namespace pma

@@ -79,11 +79,12 @@ static void run_pore_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const p
 }
 
 static void run_geo_chain(pma_ctx* ctx, const Fields& f, pma_dims dims, const pma_options& o, pma_outputs* out) {
-    const bool geo64 = o.run_geodesic && o.geodesic_fp64;
-    if (o.run_geodesic && !geo64)
-        out->n_cavities = geodesic<float>(ctx, f.solid, dims, o.stencil, f.dist32, f.cavity, out->cavities, 16);
-    else if (o.run_geodesic)
-        out->n_cavities = geodesic<double>(ctx, f.solid, dims, o.stencil, f.dist64, f.cavity, out->cavities, 16);
+    if (!o.run_geodesic) return;
+    const std::vector<pma_cavity> rows =
+        o.geodesic_fp64 ? geodesic<double>(ctx, f.solid, dims, o.stencil, f.dist64, f.cavity)
+                        : geodesic<float>(ctx, f.solid, dims, o.stencil, f.dist32, f.cavity);
+    copy_cavities(rows, out->cavities, 16, &out->n_cavities);
+    if (out->cavity_rows) copy_cavities(rows, out->cavity_rows, out->cavity_rows_cap, nullptr);
 }
 
 static pma_options options_or_default(const pma_options* opts) {
@@ -358,11 +359,10 @@ void run_one(pma_ctx* ctx, const std::string& base, pma_mode mode) {
         uint8_t* d_solid = upload(ctx, "pipe.solid", solid);
         float* dist = static_cast<float*>(ctx->scratch("pipe.dist32", n * 4));
         uint32_t* cav = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
-        pma_cavity c[64];
-        int nc = geodesic<float>(ctx, d_solid, dims, st, dist, cav, c, 64);
+        const std::vector<pma_cavity> c = geodesic<float>(ctx, d_solid, dims, st, dist, cav);
         write_field(f, kDist, dist, ctx);
         write_field(f, kCav, cav, ctx);
-        write_cavities(f, c, nc);
+        write_cavities(f, c.data(), static_cast<int>(c.size()));
         return;
     }
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <map>
@@ -84,6 +85,7 @@ struct pma_ctx {
     };
     std::vector<Timed> timed;
     std::vector<pma_ctx*> lanes;  // child contexts of batch calls (own stream and scratch)
+    pma_limits limits{1 << 20, 1 << 22, (1ull << 23) - 1, 0};  // device loop bounds
     // Demand: the largest size each named buffer was asked for since reset_demand(), summed;
     // what one request needs, whatever earlier requests left in the cache.
     std::map<std::string, size_t> demand;
@@ -150,14 +152,23 @@ void edt_noalloc(const uint8_t* solid, pma_dims d, uint32_t* edt2, pma_edt_stats
 void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t max_edt2,
                       uint32_t* crad2, uint32_t* cx, uint32_t* cy, uint32_t* cz, uint8_t* mask,
                       uint64_t* count);
+// Returns every cavity's row, in the order the cavities were flooded.
 template <class T>
-int geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
-             uint32_t* cavity, pma_cavity* cav, int cav_cap);
+std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d, pma_stencil st, T* dist,
+                                 uint32_t* cavity);
 pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const uint32_t* crad2,
                  pma_dims d, pma_stencil st, uint32_t* labels);
 void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d);
 pma_table* watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* crad2, pma_dims d,
                      pma_stencil st, uint32_t max_edt2, uint32_t* labels);
+void wait_selftest(pma_ctx* ctx, int* timed_out);
+
+// Copies the first `cap` cavity rows to `out` and reports how many there are in all.
+inline void copy_cavities(const std::vector<pma_cavity>& rows, pma_cavity* out, int cap, int* n) {
+    const size_t k = std::min(rows.size(), static_cast<size_t>(cap > 0 ? cap : 0));
+    for (size_t i = 0; i < k; ++i) out[i] = rows[i];
+    if (n) *n = static_cast<int>(rows.size());
+}
 
 // Whole chain of one volume on ctx's stream (pipeline.cpp): from host buffers, or on device
 // buffers (output field pointers of `out` are device pointers, NULL = context scratch).

@@ -41,7 +41,6 @@ namespace pma {
 namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
-constexpr int kUnionLimit = 1 << 22;
 
 __global__ void flag_outer(const uint8_t* __restrict__ mask, size_t n, uint8_t* __restrict__ flags) {
     PMA_GRID_STRIDE(v, n) flags[v] = mask[v] == 255;
@@ -153,7 +152,7 @@ __global__ void uf_jump(size_t n, uint32_t* __restrict__ parent, unsigned int* _
 }
 
 __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int d3q7,
-                        uint32_t* __restrict__ parent, unsigned int* __restrict__ err) {
+                        uint32_t* __restrict__ parent, unsigned int* __restrict__ err, int union_limit) {
     PMA_GRID_STRIDE(v, n) {
         const uint32_t r = crad[v];
         if (!r) continue;
@@ -185,7 +184,7 @@ __global__ void uf_hook(const uint32_t* __restrict__ crad, Grid g, size_t n, int
             uint32_t b = uf_root(parent, static_cast<uint32_t>(w));
             int it = 0;
             while (a != b) {
-                if (++it > kUnionLimit) {
+                if (++it > union_limit) {
                     atomicOr(err, 1u);
                     break;
                 }
@@ -287,13 +286,13 @@ __global__ void uf_pairs(const uint32_t* __restrict__ crad, Grid g, size_t n, in
 }
 
 __global__ void uf_union_pairs(const unsigned long long* __restrict__ pairs, size_t np,
-                               uint32_t* __restrict__ parent, unsigned int* __restrict__ err) {
+                               uint32_t* __restrict__ parent, unsigned int* __restrict__ err, int union_limit) {
     PMA_GRID_STRIDE(i, np) {
         uint32_t a = uf_root(parent, static_cast<uint32_t>(pairs[i] >> 32));
         uint32_t b = uf_root(parent, static_cast<uint32_t>(pairs[i]));
         int it = 0;
         while (a != b) {
-            if (++it > kUnionLimit) {
+            if (++it > union_limit) {
                 atomicOr(err, 1u);
                 break;
             }
@@ -1137,11 +1136,12 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                 pcap = npairs + npairs / 8 + 1024;
             }
             if (npairs) {
-                uf_union_pairs<<<grid_for(ctx, npairs), 256, 0, s>>>(pairs, npairs, pid, err);
+                uf_union_pairs<<<grid_for(ctx, npairs), 256, 0, s>>>(pairs, npairs, pid, err,
+                                                                      ctx->limits.union_limit);
                 ctx->check_launch("uf_union_pairs");
             }
         } else {
-            uf_hook<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid, err);
+            uf_hook<<<G, 256, 0, s>>>(crad2, g, n, d3q7, pid, err, ctx->limits.union_limit);
         }
     }
     ctx->check_launch("uf_hook");

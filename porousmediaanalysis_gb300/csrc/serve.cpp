@@ -189,6 +189,7 @@ int pma_server_create(pma_ctx* ctx, const pma_server_config* cfg, pma_server** o
                 PMA_REQUIRE(pma_ctx_create(ctx->device, &c) == PMA_OK, PMA_ERR_CUDA,
                             "pma_server_create: lane context");
                 c->blocking_sync = true;
+                c->limits = ctx->limits;
                 l.ctx = c;
             }
         } catch (...) {

@@ -25,7 +25,10 @@
 // prefix of length >= 2 was created at the time of its last extension. All prefixes are
 // hashed, grouped with radix sorts and ranked by creation time on the device, which
 // reproduces the reference's id sequence (UINT32_MAX - 1, - 2, ...) exactly, including
-// types whose volume later dropped to zero.
+// types whose volume later dropped to zero. A voxel's extending pores are kept in a chain of
+// fixed-size records, so a key may hold as many pores as the stencil lets touch one voxel
+// (the reference keys types by an unbounded pore-id vector,
+// BasePoreAndThroatComputer.cpp:112-133).
 #include <cooperative_groups.h>
 #include <thrust/iterator/counting_iterator.h>
 
@@ -41,14 +44,15 @@ namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kNoTime = ~0ull;
-constexpr int kSlots = 6;         // distinct extending pores recorded per shared voxel
-constexpr int kKey = kSlots + 1;  // longest key
+constexpr int kSlots = 6;         // extending pores per record; a voxel chains more records
+constexpr int kMaxExt = 26;       // extending pores of one voxel at most (26 neighbours touch it)
+constexpr int kMaxHops = (kMaxExt + kSlots - 1) / kSlots;  // records in one voxel's chain
+constexpr int kKeyMax = kMaxExt + 1;  // longest key: the claimer and every extending pore
 constexpr int kChunk = 1024;      // event slots per compaction block
 constexpr int kGensPerLaunch = 64;  // generations per cooperative launch (host checks between)
 constexpr unsigned long long kMaxGen = 1ull << 23;              // generations per call
 constexpr unsigned long long kSeqMask = (1ull << 40) - 1;       // touch time within a generation
 constexpr uint32_t kRecBusy = 0xFFFFFFFFu;  // ext[w] while its record is being allocated
-constexpr int kSpinLimit = 1 << 20;
 
 struct WsState {
     Grid g;
@@ -59,10 +63,12 @@ struct WsState {
     uint32_t* ext;                // shared-voxel record + 1, 0 = none
     uint32_t* ext_pore;           // [records][kSlots]
     unsigned long long* ext_time;
+    uint32_t* ext_next;           // [records]: the voxel's next record + 1, 0 = none
     unsigned int* ext_count;
     uint32_t ext_cap;
     unsigned int* pbound;         // per pore
     unsigned int* err;
+    int spin_limit;               // polls of one wait on another block before giving up
     uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
     unsigned int* bfill;
@@ -115,48 +121,54 @@ __global__ void ws_histograms(const uint32_t* __restrict__ crad, size_t n, uint3
             if (local[i]) atomicAdd(&hist[i], local[i]);
 }
 
-// Records that `pore` touched shared voxel w at time t (its first touch per pore is kept).
-// Out of line: it is the rare path of the touch kernel.
-// A voxel's record is allocated by the one touch that moves ext[w] from 0 to kRecBusy;
-// touches that meet kRecBusy wait (a few instructions) for the record number.
-__device__ __noinline__ void ws_extend(uint32_t* ext, unsigned int* ext_count, uint32_t ext_cap,
-                                       uint32_t* ext_pore, unsigned long long* ext_time, unsigned int* err,
-                                       size_t w, uint32_t pore, unsigned long long t) {
-    uint32_t rec = *reinterpret_cast<volatile uint32_t*>(ext + w);
+// The record a link (ext[w] or a record's next field) points to, allocated by the one touch
+// that moves the link from 0 to kRecBusy; touches that meet kRecBusy wait (a few
+// instructions) for the record number. Returns 0 when the records ran out (err bit 1: the
+// flood is redone with more) or the wait gave up (err bit 8).
+__device__ __forceinline__ uint32_t ws_follow(uint32_t* link, const WsState& s) {
+    uint32_t rec = *reinterpret_cast<volatile uint32_t*>(link);
     if (rec == 0) {
-        rec = atomicCAS(&ext[w], 0u, kRecBusy);
+        rec = atomicCAS(link, 0u, kRecBusy);
         if (rec == 0) {
-            const uint32_t fresh = atomicAdd(ext_count, 1u) + 1;
-            if (fresh > ext_cap) {  // out of records: give the number back, flag a redo
-                atomicSub(ext_count, 1u);
-                atomicExch(&ext[w], 0u);
-                atomicOr(err, 1u);
-                return;
+            const uint32_t fresh = atomicAdd(s.ext_count, 1u) + 1;
+            if (fresh > s.ext_cap) {  // out of records: give the number back, flag a redo
+                atomicSub(s.ext_count, 1u);
+                atomicExch(link, 0u);
+                atomicOr(s.err, 1u);
+                return 0;
             }
-            atomicExch(&ext[w], fresh);
-            rec = fresh;
+            atomicExch(link, fresh);
+            return fresh;
         }
     }
     for (int spins = 0; rec == kRecBusy; ++spins) {
-        if (spins > kSpinLimit) {
-            atomicOr(err, 8u);
-            return;
+        if (spins > s.spin_limit) {
+            atomicOr(s.err, 8u);
+            return 0;
         }
-        rec = atomicAdd(&ext[w], 0u);
+        rec = atomicAdd(link, 0u);
     }
-    if (rec == 0) {  // the allocating touch ran out of records
-        atomicOr(err, 1u);
-        return;
-    }
-    for (int k = 0; k < kSlots; ++k) {
-        const size_t slot = static_cast<size_t>(rec - 1) * kSlots + k;
-        const uint32_t cur = atomicCAS(&ext_pore[slot], kNone, pore);
-        if (cur == kNone || cur == pore) {
-            atomicMin(&ext_time[slot], t);
-            return;
+    if (rec == 0) atomicOr(s.err, 1u);  // the allocating touch ran out of records
+    return rec;
+}
+
+// Records that `pore` touched shared voxel w at time t (its first touch per pore is kept).
+// Out of line: it is the rare path of the touch kernel. Slots fill in order along the
+// voxel's record chain, so two touches by one pore meet at the same slot.
+__device__ __noinline__ void ws_extend(const WsState& s, size_t w, uint32_t pore, unsigned long long t) {
+    uint32_t rec = ws_follow(s.ext + w, s);
+    for (int hop = 0; hop < kMaxHops && rec; ++hop) {
+        for (int k = 0; k < kSlots; ++k) {
+            const size_t slot = static_cast<size_t>(rec - 1) * kSlots + k;
+            const uint32_t cur = atomicCAS(&s.ext_pore[slot], kNone, pore);
+            if (cur == kNone || cur == pore) {
+                atomicMin(&s.ext_time[slot], t);
+                return;
+            }
         }
+        if (hop + 1 < kMaxHops) rec = ws_follow(s.ext_next + (rec - 1), s);
     }
-    atomicOr(err, 2u);
+    if (rec) atomicOr(s.err, 2u);  // more extending pores than neighbours: cannot happen
 }
 
 // Touch events of the generation's nodes. Phase 0 claims: the smallest touch time of each
@@ -197,7 +209,7 @@ __device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t*
                     atomicMin(&s.ckey[w], (tag << 40) | seq);
                     touched = 1;
                 } else if (c - 1 != pore) {
-                    ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
+                    ws_extend(s, w, pore, (gen << 40) | seq);
                 }
             }
         }
@@ -238,8 +250,7 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
         return false;
     }
     const uint32_t owner = __ldcg(gp + wseq / 27);
-    if (owner != pore)
-        ws_extend(s.ext, s.ext_count, s.ext_cap, s.ext_pore, s.ext_time, s.err, w, pore, (gen << 40) | seq);
+    if (owner != pore) ws_extend(s, w, pore, (gen << 40) | seq);
     return false;
 }
 
@@ -261,7 +272,8 @@ constexpr unsigned long long kDescVal = (1ull << 38) - 1;
 
 // Called by all 32 lanes of one warp; returns the exclusive prefix of chunk c.
 __device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned long long c, unsigned long long gen,
-                                          unsigned long long own, unsigned int* err, unsigned lane) {
+                                          unsigned long long own, unsigned int* err, int spin_limit,
+                                          unsigned lane) {
     volatile unsigned long long* vd = desc;
     const unsigned long long tg = gen << 40;
     if (lane == 0) vd[c] = tg | (c == 0 ? kDescIncl : kDescOwn) | own;
@@ -276,7 +288,7 @@ __device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned lon
         const unsigned long long d = valid ? vd[p] : 0ull;
         const bool ready = !valid || (d >> 40) == gen;
         if (!__all_sync(0xFFFFFFFFu, ready)) {  // a predecessor has not published yet
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 if (lane == 0) atomicOr(err, 16u);
                 break;
             }
@@ -296,6 +308,13 @@ __device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned lon
         vd[c] = tg | kDescIncl | (excl + own);
     }
     return excl;
+}
+
+// A look-back at a chunk descriptor that nothing publishes (chunk 0 of generation 0 while
+// chunk 1 of generation 1 waits for it): the bounded wait of the frontier compaction runs
+// out after spin_limit polls and sets err bit 16, the path a stalled generation would take.
+__global__ void ws_wait_selftest(unsigned long long* desc, unsigned int* err, int spin_limit) {
+    ws_lookback(desc, 1, 1, 0, err, spin_limit, threadIdx.x & 31);
 }
 
 // Up to max_gens generations of one depth in a single cooperative launch, two grid-wide
@@ -349,7 +368,7 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
                 }
                 const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
                 part[lane] = incl - v;
-                const unsigned long long base = ws_lookback(desc, c, gen, total, s.err, lane);
+                const unsigned long long base = ws_lookback(desc, c, gen, total, s.err, s.spin_limit, lane);
                 if (lane == 0) {
                     part[32] = static_cast<unsigned int>(base);
                     if (c == nchunks - 1) ng[cur ^ 1] = static_cast<unsigned int>(base + total);
@@ -441,27 +460,55 @@ __global__ void ws_volumes(const uint32_t* __restrict__ claim, const uint32_t* _
 
 // --- shared types -------------------------------------------------------------------------
 
-// Key of shared voxel i: [first extension, claimer, later extensions...] in pore indices,
-// and one record per prefix of length L = 2..len (record i * kSlots + L - 2).
-__global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const uint32_t* __restrict__ claim,
-                        const uint32_t* __restrict__ ext, const uint32_t* __restrict__ ext_pore,
-                        const unsigned long long* __restrict__ ext_time, uint32_t* __restrict__ kseq,
-                        uint8_t* __restrict__ klen, unsigned long long* __restrict__ rh1,
-                        unsigned long long* __restrict__ rh2, unsigned long long* __restrict__ rtime,
-                        uint8_t* __restrict__ rvalid) {
-    PMA_GRID_STRIDE(i, ns) {
-        const uint32_t v = sv[i];
-        const uint32_t rec = ext[v] - 1;
-        uint32_t p[kSlots];
-        unsigned long long t[kSlots];
-        int m = 0;
+// Extending pores of the shared voxel whose chain starts at record `rec`, with their first
+// touch times, in slot order; returns how many (at most kMaxExt).
+__device__ __forceinline__ int ws_chain(const uint32_t* __restrict__ ext_pore,
+                                        const unsigned long long* __restrict__ ext_time,
+                                        const uint32_t* __restrict__ ext_next, uint32_t rec, uint32_t* p,
+                                        unsigned long long* t) {
+    int m = 0;
+    for (int hop = 0; hop < kMaxHops && rec != 0 && rec != kRecBusy; ++hop) {
         for (int k = 0; k < kSlots; ++k) {
-            const uint32_t pk = ext_pore[static_cast<size_t>(rec) * kSlots + k];
-            if (pk == kNone) continue;
-            p[m] = pk;
-            t[m] = ext_time[static_cast<size_t>(rec) * kSlots + k];
+            const size_t slot = static_cast<size_t>(rec - 1) * kSlots + k;
+            const uint32_t pk = ext_pore[slot];
+            if (pk == kNone) return m;
+            if (p) {
+                p[m] = pk;
+                t[m] = ext_time[slot];
+            }
             ++m;
         }
+        rec = ext_next[rec - 1];
+    }
+    return m;
+}
+
+// Key length (claimer + extending pores) of each shared voxel, for the offsets of its key and
+// of its prefix records.
+__global__ void ws_key_lengths(const uint32_t* __restrict__ sv, size_t ns, const uint32_t* __restrict__ ext,
+                               const uint32_t* __restrict__ ext_pore, const uint32_t* __restrict__ ext_next,
+                               uint8_t* __restrict__ klen, unsigned long long* __restrict__ klen64) {
+    PMA_GRID_STRIDE(i, ns) {
+        const int len = ws_chain(ext_pore, nullptr, ext_next, ext[sv[i]], nullptr, nullptr) + 1;
+        klen[i] = static_cast<uint8_t>(len);
+        klen64[i] = static_cast<unsigned long long>(len);
+    }
+}
+
+// Key of shared voxel i: [first extension, claimer, later extensions...] in pore indices, at
+// kseq[koff[i] ..], and one record per prefix of length L = 2..len at record
+// koff[i] - i + L - 2 (its hashes, creation time and voxel).
+__global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const uint32_t* __restrict__ claim,
+                        const uint32_t* __restrict__ ext, const uint32_t* __restrict__ ext_pore,
+                        const unsigned long long* __restrict__ ext_time, const uint32_t* __restrict__ ext_next,
+                        const unsigned long long* __restrict__ koff, uint32_t* __restrict__ kseq,
+                        unsigned long long* __restrict__ rh1, unsigned long long* __restrict__ rh2,
+                        unsigned long long* __restrict__ rtime, uint32_t* __restrict__ rvox) {
+    PMA_GRID_STRIDE(i, ns) {
+        const uint32_t v = sv[i];
+        uint32_t p[kMaxExt];
+        unsigned long long t[kMaxExt];
+        const int m = ws_chain(ext_pore, ext_time, ext_next, ext[v], p, t);
         for (int a = 1; a < m; ++a)  // insertion sort by time
             for (int b = a; b > 0 && t[b] < t[b - 1]; --b) {
                 const unsigned long long tt = t[b];
@@ -471,27 +518,28 @@ __global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const uint32
                 p[b] = p[b - 1];
                 p[b - 1] = pp;
             }
-        uint32_t key[kKey];
+        uint32_t key[kKeyMax];
         key[0] = p[0];
         key[1] = claim[v] - 1;
         for (int k = 1; k < m; ++k) key[k + 1] = p[k];
         const int len = m + 1;
-        for (int k = 0; k < kKey; ++k) kseq[i * kKey + k] = k < len ? key[k] : kNone;
-        klen[i] = static_cast<uint8_t>(len);
-        for (int L = 2; L <= kKey; ++L) {
-            const size_t r = i * kSlots + (L - 2);
-            if (L <= len) {
-                unsigned long long a, b;
-                list_hash(key, static_cast<uint32_t>(L), a, b);
-                rh1[r] = a;
-                rh2[r] = b;
-                rtime[r] = t[L - 2];
-                rvalid[r] = 1;
-            } else {
-                rvalid[r] = 0;
-            }
+        const unsigned long long base = koff[i];
+        for (int k = 0; k < len; ++k) kseq[base + k] = key[k];
+        const unsigned long long rbase = base - i;
+        for (int L = 2; L <= len; ++L) {
+            const unsigned long long r = rbase + (L - 2);
+            unsigned long long h1, h2;
+            list_hash(key, static_cast<uint32_t>(L), h1, h2);
+            rh1[r] = h1;
+            rh2[r] = h2;
+            rtime[r] = t[L - 2];
+            rvox[r] = static_cast<uint32_t>(i);
         }
     }
+}
+
+__global__ void ws_iota(uint32_t* __restrict__ a, size_t n) {
+    PMA_GRID_STRIDE(i, n) a[i] = static_cast<uint32_t>(i);
 }
 
 __global__ void ws_gather_h(const unsigned long long* __restrict__ h, const uint32_t* __restrict__ idx,
@@ -499,11 +547,27 @@ __global__ void ws_gather_h(const unsigned long long* __restrict__ h, const uint
     PMA_GRID_STRIDE(i, n) out[i] = h[idx[i]];
 }
 
+// Prefix record r: its voxel, the start of that voxel's key and the prefix length.
+struct RecRef {
+    uint32_t vi;
+    unsigned long long kbase;
+    uint32_t L;
+};
+
+__device__ __forceinline__ RecRef ws_rec(uint32_t r, const uint32_t* __restrict__ rvox,
+                                         const unsigned long long* __restrict__ koff) {
+    RecRef x;
+    x.vi = rvox[r];
+    x.kbase = koff[x.vi];
+    x.L = static_cast<uint32_t>(r - (x.kbase - x.vi)) + 2u;
+    return x;
+}
+
 __global__ void ws_group_starts(const uint32_t* __restrict__ rec, size_t nr,
                                 const unsigned long long* __restrict__ rh1,
-                                const unsigned long long* __restrict__ rh2,
-                                const uint32_t* __restrict__ kseq, uint32_t* __restrict__ start,
-                                unsigned int* __restrict__ err) {
+                                const unsigned long long* __restrict__ rh2, const uint32_t* __restrict__ kseq,
+                                const unsigned long long* __restrict__ koff, const uint32_t* __restrict__ rvox,
+                                uint32_t* __restrict__ start, unsigned int* __restrict__ err) {
     PMA_GRID_STRIDE(i, nr) {
         const uint32_t r = rec[i];
         bool s = i == 0;
@@ -511,10 +575,9 @@ __global__ void ws_group_starts(const uint32_t* __restrict__ rec, size_t nr,
             const uint32_t q = rec[i - 1];
             s = rh1[r] != rh1[q] || rh2[r] != rh2[q];
             if (!s) {  // verify: same prefix
-                const uint32_t L = r % kSlots + 2, Lq = q % kSlots + 2;
-                bool eq = L == Lq;
-                for (uint32_t k = 0; eq && k < L; ++k)
-                    eq = kseq[(r / kSlots) * kKey + k] == kseq[(q / kSlots) * kKey + k];
+                const RecRef a = ws_rec(r, rvox, koff), b = ws_rec(q, rvox, koff);
+                bool eq = a.L == b.L;
+                for (uint32_t k = 0; eq && k < a.L; ++k) eq = kseq[a.kbase + k] == kseq[b.kbase + k];
                 if (!eq) atomicOr(err, 4u);
             }
         }
@@ -525,16 +588,17 @@ __global__ void ws_group_starts(const uint32_t* __restrict__ rec, size_t nr,
 __global__ void ws_group_reduce(const uint32_t* __restrict__ rec, const uint32_t* __restrict__ excl,
                                 const uint32_t* __restrict__ start, size_t nr,
                                 const unsigned long long* __restrict__ rtime, const uint8_t* __restrict__ klen,
+                                const unsigned long long* __restrict__ koff, const uint32_t* __restrict__ rvox,
                                 unsigned long long* __restrict__ gtime, unsigned long long* __restrict__ gvol,
                                 uint32_t* __restrict__ grep, uint32_t* __restrict__ final_group) {
     PMA_GRID_STRIDE(i, nr) {
         const uint32_t r = rec[i];
         const uint32_t g = excl[i] + start[i] - 1u;
         atomicMin(&gtime[g], rtime[r]);
-        const uint32_t vi = r / kSlots, L = r % kSlots + 2;
-        if (L == klen[vi]) {
+        const RecRef a = ws_rec(r, rvox, koff);
+        if (a.L == klen[a.vi]) {
             atomicAdd(&gvol[g], 1ull);
-            final_group[vi] = g;
+            final_group[a.vi] = g;
         }
         if (start[i]) grep[g] = r;
     }
@@ -554,11 +618,11 @@ __global__ void ws_shared_labels(const uint32_t* __restrict__ sv, const uint32_t
 }
 
 __global__ void ws_group_rows(const uint32_t* __restrict__ grep, size_t ngr, const uint32_t* __restrict__ kseq,
+                              const unsigned long long* __restrict__ koff, const uint32_t* __restrict__ rvox,
                               uint32_t* __restrict__ out) {
     PMA_GRID_STRIDE(g, ngr) {
-        const uint32_t r = grep[g];
-        const uint32_t L = r % kSlots + 2, vi = r / kSlots;
-        for (int k = 0; k < kKey; ++k) out[g * kKey + k] = k < static_cast<int>(L) ? kseq[vi * kKey + k] : kNone;
+        const RecRef a = ws_rec(grep[g], rvox, koff);
+        for (uint32_t k = 0; k < kKeyMax; ++k) out[g * kKeyMax + k] = k < a.L ? kseq[a.kbase + k] : kNone;
     }
 }
 
@@ -612,11 +676,12 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ws.ext = buf<uint32_t>(ctx, "ws.ext", n);
     ws.ext_count = reinterpret_cast<unsigned int*>(d_count + 1);
     ws.err = reinterpret_cast<unsigned int*>(d_count + 2);
+    ws.spin_limit = ctx->limits.spin_limit;
     ws.pbound = buf<unsigned int>(ctx, "ws.pbound", npores);
     // Shared-voxel records: a first guess of n/32; the pool doubles (copying the records)
     // whenever it is more than half used at a host synchronisation point, and a flood that
-    // still runs out is redone with four times as many (up to one per voxel).
-    const size_t max_records = std::min<size_t>(n + 4096, 0x7FFFFFFF / kSlots);
+    // still runs out is redone with four times as many (up to two per voxel).
+    const size_t max_records = std::min<size_t>(2 * n + 4096, 0x7FFFFFFF / kSlots);
     size_t ext_cap = std::min<size_t>(std::max<size_t>(n / 32, 4096), max_records);
     int ext_side = 0;  // which of two scratch tags holds the records
     auto ext_tag = [&](const char* base) { return std::string(base) + (ext_side ? ".1" : ".0"); };
@@ -624,18 +689,24 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         if (2 * used <= ws.ext_cap || ws.ext_cap >= max_records) return;
         const size_t old_cap = ws.ext_cap;
         const size_t cap2 = std::min<size_t>(std::max<size_t>(2 * old_cap, 4 * used), max_records);
-        const std::string old_p = ext_tag("ws.ext_pore"), old_t = ext_tag("ws.ext_time");
+        const std::string old_p = ext_tag("ws.ext_pore"), old_t = ext_tag("ws.ext_time"),
+                          old_n = ext_tag("ws.ext_next");
         ext_side ^= 1;
         auto* np_ = buf<uint32_t>(ctx, ext_tag("ws.ext_pore").c_str(), cap2 * kSlots);
         auto* nt_ = buf<unsigned long long>(ctx, ext_tag("ws.ext_time").c_str(), cap2 * kSlots);
+        auto* nn_ = buf<uint32_t>(ctx, ext_tag("ws.ext_next").c_str(), cap2);
         PMA_CUDA(cudaMemcpyAsync(np_, ws.ext_pore, old_cap * kSlots * 4, cudaMemcpyDeviceToDevice, s));
         PMA_CUDA(cudaMemcpyAsync(nt_, ws.ext_time, old_cap * kSlots * 8, cudaMemcpyDeviceToDevice, s));
+        PMA_CUDA(cudaMemcpyAsync(nn_, ws.ext_next, old_cap * 4, cudaMemcpyDeviceToDevice, s));
         PMA_CUDA(cudaMemsetAsync(np_ + old_cap * kSlots, 0xFF, (cap2 - old_cap) * kSlots * 4, s));
         PMA_CUDA(cudaMemsetAsync(nt_ + old_cap * kSlots, 0xFF, (cap2 - old_cap) * kSlots * 8, s));
+        PMA_CUDA(cudaMemsetAsync(nn_ + old_cap, 0, (cap2 - old_cap) * 4, s));
         ctx->release(old_p);
         ctx->release(old_t);
+        ctx->release(old_n);
         ws.ext_pore = np_;
         ws.ext_time = nt_;
+        ws.ext_next = nn_;
         ws.ext_cap = static_cast<uint32_t>(cap2);
     };
     unsigned int h_err = 0;
@@ -645,6 +716,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         ws.ext_pore = buf<uint32_t>(ctx, ext_tag("ws.ext_pore").c_str(), static_cast<size_t>(ws.ext_cap) * kSlots);
         ws.ext_time = buf<unsigned long long>(ctx, ext_tag("ws.ext_time").c_str(),
                                               static_cast<size_t>(ws.ext_cap) * kSlots);
+        ws.ext_next = buf<uint32_t>(ctx, ext_tag("ws.ext_next").c_str(), ws.ext_cap);
+        PMA_CUDA(cudaMemsetAsync(ws.ext_next, 0, static_cast<size_t>(ws.ext_cap) * 4, s));
         PMA_CUDA(cudaMemsetAsync(d_count, 0, 32, s));
         PMA_CUDA(cudaMemsetAsync(ws.ext_pore, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 4, s));
         PMA_CUDA(cudaMemsetAsync(ws.ext_time, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 8, s));
@@ -720,6 +793,9 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         const unsigned coop_grid = static_cast<unsigned>(
             std::max<size_t>(1, std::min<size_t>(coop_need, static_cast<size_t>(ctx->num_sms) * std::min(per_sm, 8))));
         unsigned long long gen = 0;
+        // generations of this call at most: the context's bound, below the claim-key tag range
+        const unsigned long long max_gen =
+            std::min<unsigned long long>(ctx->limits.watershed_generations, kMaxGen - 1);
         unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
         auto* d_out = buf<unsigned long long>(ctx, "ws.coop_out", 2);
         unsigned long long* h_out = reinterpret_cast<unsigned long long*>(h_small + 8);
@@ -760,7 +836,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
             KernelTimer kt(ctx, "ws_generations");
             while (true) {
                 const uint32_t dep = static_cast<uint32_t>(depth);
-                int gens = kGensPerLaunch;
+                PMA_REQUIRE(gen < max_gen, PMA_ERR_LIMIT, "pma_watershed: generation limit reached");
+                int gens = static_cast<int>(std::min<unsigned long long>(kGensPerLaunch, max_gen - gen));
                 void* args[] = {&ws, &gvb[0], &gpb[0], &gvb[1], &gpb[1], &d_ng, &desc,
                                 const_cast<uint32_t*>(&dep), &gen, &gens, &cur, &d_out};
                 PMA_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ws_generations), coop_grid,
@@ -779,7 +856,6 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
                 cur = static_cast<int>(h_out[1]);
                 grow_records(h_small[4]);
                 if (h_small[6 + cur] == 0) break;
-                PMA_REQUIRE(gen + kGensPerLaunch < kMaxGen, PMA_ERR_LIMIT, "pma_watershed: generation limit reached");
             }
             if (next_depth >= 0) {
                 n0 = h_small[0];
@@ -792,7 +868,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         PMA_REQUIRE(start_cap < max_records, PMA_ERR_MEMORY, "pma_watershed: shared-voxel records exhausted");
         ext_cap = std::min<size_t>(std::max<size_t>(ws.ext_cap, start_cap * 4), max_records);
     }
-    PMA_REQUIRE(!(h_err & 2u), PMA_ERR_LIMIT, "pma_watershed: more than 7 pores touch one voxel");
+    PMA_REQUIRE(!(h_err & 2u), PMA_ERR_INTERNAL, "pma_watershed: a shared voxel recorded more pores than touch it");
     PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
     PMA_REQUIRE(!(h_err & 16u), PMA_ERR_LIMIT, "pma_watershed: frontier compaction look-back did not finish");
 
@@ -829,34 +905,44 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     }
     if (nsh == 0) return t;
 
-    // Shared types on the device.
-    const size_t nrec = static_cast<size_t>(nsh) * kSlots;
-    PMA_REQUIRE(nrec < 0xFFFFFFFFull, PMA_ERR_LIMIT, "pma_watershed: too many shared voxels");
-    uint32_t* kseq = buf<uint32_t>(ctx, "ws.kseq", static_cast<size_t>(nsh) * kKey);
+    // Shared types on the device: key lengths, key and prefix-record offsets, keys and
+    // prefix records, then the prefixes grouped by hash and ranked by creation time.
     uint8_t* klen = buf<uint8_t>(ctx, "ws.klen", nsh);
-    auto* rh1 = buf<unsigned long long>(ctx, "ws.rh1", nrec);
-    auto* rh2 = buf<unsigned long long>(ctx, "ws.rh2", nrec);
-    auto* rtime = buf<unsigned long long>(ctx, "ws.rtime", nrec);
-    uint8_t* rvalid = buf<uint8_t>(ctx, "ws.rvalid", nrec);
-    ws_keys<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.claim, ws.ext, ws.ext_pore, ws.ext_time, kseq,
-                                               klen, rh1, rh2, rtime, rvalid);
+    auto* klen64 = buf<unsigned long long>(ctx, "ws.klen64", nsh);
+    auto* koff = buf<unsigned long long>(ctx, "ws.koff", nsh);
+    ws_key_lengths<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.ext, ws.ext_pore, ws.ext_next, klen, klen64);
+    ctx->check_launch("ws_key_lengths");
+    exclusive_sum(ctx, klen64, koff, nsh);
+    unsigned long long kl[2] = {0, 0};
+    PMA_CUDA(cudaMemcpyAsync(&kl[0], koff + nsh - 1, 8, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(&kl[1], klen64 + nsh - 1, 8, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    const unsigned long long nkey = kl[0] + kl[1];      // key elements of all shared voxels
+    const unsigned long long nrec_u = nkey - static_cast<unsigned long long>(nsh);  // prefixes
+    PMA_REQUIRE(nrec_u < 0xFFFFFFFFull, PMA_ERR_LIMIT, "pma_watershed: too many shared voxels");
+    const int64_t nr = static_cast<int64_t>(nrec_u);
+    uint32_t* kseq = buf<uint32_t>(ctx, "ws.kseq", nkey);
+    auto* rh1 = buf<unsigned long long>(ctx, "ws.rh1", nr);
+    auto* rh2 = buf<unsigned long long>(ctx, "ws.rh2", nr);
+    auto* rtime = buf<unsigned long long>(ctx, "ws.rtime", nr);
+    uint32_t* rvox = buf<uint32_t>(ctx, "ws.rvox", nr);
+    ws_keys<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.claim, ws.ext, ws.ext_pore, ws.ext_time, ws.ext_next,
+                                               koff, kseq, rh1, rh2, rtime, rvox);
     ctx->check_launch("ws_keys");
-    uint32_t* rec = buf<uint32_t>(ctx, "ws.rec", nrec);
-    const int64_t nr = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), rvalid, rec,
-                                      static_cast<int64_t>(nrec), d_count);
+    uint32_t* rec = buf<uint32_t>(ctx, "ws.rec", nr);
+    uint32_t* rec2 = buf<uint32_t>(ctx, "ws.rec2", nr);
+    ws_iota<<<grid_for(ctx, nr), 256, 0, s>>>(rec, nr);
+    ctx->check_launch("ws_iota");
     // equal prefixes become adjacent: stable sorts by h2, then by h1 (values: record ids)
     auto* kh = buf<unsigned long long>(ctx, "ws.kh", nr);
     auto* kh2 = buf<unsigned long long>(ctx, "ws.kh2", nr);
-    uint32_t* rec2 = buf<uint32_t>(ctx, "ws.rec2", nr);
-    ws_gather_h<<<grid_for(ctx, nr), 256, 0, s>>>(rh2, rec, nr, kh);
-    ctx->check_launch("ws_gather_h");
-    sort_pairs(ctx, kh, kh2, rec, rec2, nr);
+    sort_pairs(ctx, rh2, kh2, rec, rec2, nr);
     ws_gather_h<<<grid_for(ctx, nr), 256, 0, s>>>(rh1, rec2, nr, kh);
     ctx->check_launch("ws_gather_h");
     sort_pairs(ctx, kh, kh2, rec2, rec, nr);
     uint32_t* gstart = buf<uint32_t>(ctx, "ws.gstart", nr);
     uint32_t* gexcl = buf<uint32_t>(ctx, "ws.gexcl", nr);
-    ws_group_starts<<<grid_for(ctx, nr), 256, 0, s>>>(rec, nr, rh1, rh2, kseq, gstart, ws.err);
+    ws_group_starts<<<grid_for(ctx, nr), 256, 0, s>>>(rec, nr, rh1, rh2, kseq, koff, rvox, gstart, ws.err);
     ctx->check_launch("ws_group_starts");
     exclusive_sum(ctx, gstart, gexcl, nr);
     uint32_t last[2] = {0, 0};
@@ -872,14 +958,14 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     uint32_t* final_group = buf<uint32_t>(ctx, "ws.fgroup", nsh);
     PMA_CUDA(cudaMemsetAsync(gtime, 0xFF, ngr * 8, s));
     PMA_CUDA(cudaMemsetAsync(gvol, 0, ngr * 8, s));
-    ws_group_reduce<<<grid_for(ctx, nr), 256, 0, s>>>(rec, gexcl, gstart, nr, rtime, klen, gtime, gvol, grep,
-                                                      final_group);
+    ws_group_reduce<<<grid_for(ctx, nr), 256, 0, s>>>(rec, gexcl, gstart, nr, rtime, klen, koff, rvox, gtime,
+                                                      gvol, grep, final_group);
     ctx->check_launch("ws_group_reduce");
-    uint32_t* rows = buf<uint32_t>(ctx, "ws.rows", static_cast<size_t>(ngr) * kKey);
-    ws_group_rows<<<grid_for(ctx, ngr), 256, 0, s>>>(grep, ngr, kseq, rows);
+    uint32_t* rows = buf<uint32_t>(ctx, "ws.rows", static_cast<size_t>(ngr) * kKeyMax);
+    ws_group_rows<<<grid_for(ctx, ngr), 256, 0, s>>>(grep, ngr, kseq, koff, rvox, rows);
     ctx->check_launch("ws_group_rows");
     std::vector<unsigned long long> h_gtime(ngr), h_gvol(ngr);
-    std::vector<uint32_t> h_rows(static_cast<size_t>(ngr) * kKey);
+    std::vector<uint32_t> h_rows(static_cast<size_t>(ngr) * kKeyMax);
     PMA_CUDA(cudaMemcpyAsync(h_gtime.data(), gtime, ngr * 8, cudaMemcpyDeviceToHost, s));
     PMA_CUDA(cudaMemcpyAsync(h_gvol.data(), gvol, ngr * 8, cudaMemcpyDeviceToHost, s));
     PMA_CUDA(cudaMemcpyAsync(h_rows.data(), rows, h_rows.size() * 4, cudaMemcpyDeviceToHost, s));
@@ -907,12 +993,25 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         th.volume = h_gvol[gi];
         th.pool_offset = t->pool.size();
         uint32_t L = 0;
-        for (int j = 0; j < kKey && h_rows[static_cast<size_t>(gi) * kKey + j] != kNone; ++j, ++L)
-            t->pool.push_back(pore_id[h_rows[static_cast<size_t>(gi) * kKey + j]]);
+        for (int j = 0; j < kKeyMax && h_rows[static_cast<size_t>(gi) * kKeyMax + j] != kNone; ++j, ++L)
+            t->pool.push_back(pore_id[h_rows[static_cast<size_t>(gi) * kKeyMax + j]]);
         th.n_pores = L;
         t->throats.push_back(th);
     }
     return t;
+}
+
+void wait_selftest(pma_ctx* ctx, int* timed_out) {
+    unsigned long long* desc = buf<unsigned long long>(ctx, "ws.selftest", 3);
+    unsigned int* err = reinterpret_cast<unsigned int*>(desc + 2);
+    PMA_CUDA(cudaMemsetAsync(desc, 0, 3 * 8, ctx->stream));
+    ws_wait_selftest<<<1, 32, 0, ctx->stream>>>(desc, err, ctx->limits.spin_limit);
+    ctx->count_launch();
+    ctx->check_launch("ws_wait_selftest");
+    unsigned int h = 0;
+    PMA_CUDA(cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    *timed_out = (h & 16u) ? 1 : 0;
 }
 
 }  // namespace pma

@@ -110,6 +110,27 @@ def grf(shape=(512, 512, 512), sigma=3.0, porosity=0.65, seed=2, device=None):
     return (f <= t).to(torch.uint8)
 
 
+def grf_exact(shape=(512, 512, 512), sigma=3.0, porosity=0.65, seed=2):
+    """Thresholded Gaussian random field computed in exact arithmetic, so that every machine
+    builds the same volume bit for bit (the parity fixtures of the 512^3 workload are taken on
+    one machine and checked on another). N(0,1) voxels are rounded to multiples of 1/256 and
+    blurred with integer weights round(1024 exp(-k^2 / 2 sigma^2)), |k| <= round(4 sigma),
+    along each axis (reflect mode, the edge sample repeated); every partial sum is an integer
+    below 2^53, so float64 holds it exactly whatever the order of the additions. Solid where
+    the field is at or below its k-th smallest value, k = floor((1 - porosity) * voxels)."""
+    from scipy import ndimage
+    rng = np.random.default_rng(seed)
+    f = np.rint(rng.standard_normal(shape) * 256.0)
+    rad = int(4 * sigma + 0.5)
+    w = np.rint(1024.0 * np.exp(-0.5 * (np.arange(-rad, rad + 1) / sigma) ** 2))
+    assert np.abs(f).max() * w.sum() ** 3 < 2.0 ** 53
+    for axis in range(3):
+        f = ndimage.correlate1d(f, w, axis=axis, mode="reflect")
+    k = int((1.0 - porosity) * f.size)
+    t = np.partition(f.reshape(-1), k)[k]
+    return (f <= t).astype(np.uint8)
+
+
 def spinodal(shape=(1024, 1024, 1024), waves=1000, wavelength=48.0, porosity=0.70, seed=3,
              device=None, chunk=16):
     """Leveled-wave monolith: f = sum_i cos(k_i . x + phi_i); void where f exceeds its

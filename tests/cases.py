@@ -60,3 +60,18 @@ def large_case():
     """2^24 voxels (256^3): the size from which plateaus are labelled by pointer jumping and
     unions of recorded parent pairs. A union of 6000 spheres, radii U[4, 12]."""
     return synth.sphere_union((256, 256, 256), count=6000, rmin=4.0, rmax=12.0, seed=77)
+
+
+def many_pockets(count=900, shape=(100, 110, 96), seed=13):
+    """A solid block holding `count` small spherical voids, none reaching more than a few
+    walls, so that the geodesic stage restarts again and again (49 cavities with the
+    defaults; a restart searches shells from one beyond the previous one, so the count is
+    bounded by the half-extent of the volume)."""
+    rng = np.random.default_rng(seed)
+    s = np.ones(shape, np.uint8)
+    zz, xx, yy = np.ogrid[:shape[0], :shape[1], :shape[2]]
+    for _ in range(count):
+        c = rng.uniform(0, 1, 3) * np.array(shape)
+        r = rng.uniform(1.0, 2.5)
+        s[(zz - c[0]) ** 2 + (xx - c[1]) ** 2 + (yy - c[2]) ** 2 <= r * r] = 0
+    return s

@@ -1,6 +1,7 @@
 """Generates the golden fixtures of tests/golden/ from the reference itself.
 
-Run once in a container that holds the reference tree (default /root/reference):
+Run once in a container that holds the reference tree (the first argument, else
+$PMA_REFERENCE_DIR, else /root/reference):
     oracle/build_ref.sh && python tests/golden/make_golden.py [reference_dir]
 
 Outputs (small, committed):
@@ -96,4 +97,4 @@ def main(ref_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PMA_REFERENCE_DIR", "/root/reference"))

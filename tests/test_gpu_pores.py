@@ -151,3 +151,39 @@ def test_pores_and_watershed_large_volume_matches_oracle_fixture(ctx):
     assert digest(canonical_throats(g["labels"])) == rec["labels_canonical"]
     assert digest(g["ws"]) == rec["labels_ws"]
     assert g["ws_table"] == (rows(rec["pores_ws"]), rows(rec["throats_ws"]))
+
+
+def _junction(n_seeds, seed):
+    """A void box whose centre voxel is touched by `n_seeds` pores seeded on its neighbours:
+    containing radii 50 around a centre of radius 1, so that every seed's first generation
+    reaches the centre (one claim, n_seeds - 1 extensions: a shared type of n_seeds pores).
+    Other voxels get random radii below 50, so the flood also runs over several depths."""
+    rng = np.random.default_rng(seed)
+    crad = rng.integers(1, 50, (9, 11, 10)).astype(np.uint32)
+    c = (4, 5, 5)  # z, x, y
+    crad[c[0] - 1:c[0] + 2, c[1] - 1:c[1] + 2, c[2] - 1:c[2] + 2] = 50
+    crad[c] = 1
+    offs = [(dx, dy, dz) for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)
+            if (dx, dy, dz) != (0, 0, 0)]
+    pick = rng.permutation(len(offs))[:n_seeds]
+    ids = [127 + k for k in range(n_seeds)]
+    rng.shuffle(ids)
+    rows = [(ids[k], c[1] + offs[i][0], c[2] + offs[i][1], c[0] + offs[i][2], 50, 0, 0)
+            for k, i in enumerate(pick)]
+    return crad, rows
+
+
+@pytest.mark.parametrize("n_seeds,seed", [(8, 1), (12, 2), (19, 3), (26, 4)])
+def test_watershed_junction_of_many_pores(ctx, oracle_mod, n_seeds, seed):
+    """Up to 26 pores meet at one voxel (the reference keys shared types by an unbounded
+    pore-id vector): labels and both tables equal the oracle's, including the type of all
+    n_seeds pores."""
+    import torch
+    import porousmediaanalysis_gb300 as pma
+    crad, rows_in = _junction(n_seeds, seed)
+    o_ws, o_pores, o_throats = oracle_mod.watershed(rows_in, crad, 50)
+    assert max(len(t[2]) for t in o_throats) == n_seeds
+    table = pma.Table.from_rows(rows_in)
+    ws, ws_table = pma.assign_watershed_ids(ctx, table, torch.from_numpy(crad.view(np.int32)).cuda(), 50)
+    assert (ws.cpu().numpy().view(np.uint32) == o_ws).all()
+    assert ws_table.rows() == (o_pores, o_throats)

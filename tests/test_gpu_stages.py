@@ -178,3 +178,24 @@ def test_containing_balls_wide_radius_span(ctx, oracle_mod):
     vol[0, 0, 0] = 1
     vol[27, 11, 38] = 1
     _balls_vs_oracle(ctx, oracle_mod, vol)
+
+
+def test_every_cavity_row_is_returned(ctx, oracle_mod):
+    """49 cavities, more than the 16 rows of pma_outputs.cavities: the stage call, the
+    host-buffer pipeline (through its cavity_rows buffer) and a count-only call all report
+    every cavity, with the oracle's rows."""
+    import torch
+    import porousmediaanalysis_gb300 as pma
+    from cases import many_pockets
+    vol = many_pockets()
+    od, oc, orows = oracle_mod.geodesic(vol)
+    assert len(orows) > 40 and not any(r[7] for r in orows)
+    solid = torch.from_numpy(vol).cuda()
+    d, c, got = pma.compute_shortest_path_distances(ctx, solid)
+    assert [cavity_key(r) for r in got] == [cavity_key(r) for r in orows]
+    assert (d.cpu().numpy().view(np.uint32) == od.view(np.uint32)).all()
+    assert (c.cpu().numpy().view(np.uint32) == oc).all()
+    _, _, first, n = pma.shortest_path_with_count(ctx, solid, cavity_cap=5)
+    assert n == len(orows) and [cavity_key(r) for r in first] == [cavity_key(r) for r in orows[:5]]
+    res = pma.pipeline_host(ctx, vol, run_pores=False, fields=("dist_f32",))
+    assert [cavity_key(r) for r in res["cavities"]] == [cavity_key(r) for r in orows]

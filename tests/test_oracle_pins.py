@@ -86,14 +86,17 @@ def test_example_pores_match_shipped_up_to_ids(example_golden):
     assert len(ship["pores_ws"]) == len(one["pores_ws"])
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/Docs/Example"),
+REFERENCE = os.environ.get("PMA_REFERENCE_DIR", "/root/reference")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "Docs", "Example")),
                     reason="needs the reference tree (fixture-generation container only)")
 def test_shipped_coordinates_are_valid_winners(oracle_mod):
     """Where the shipped (7-thread) winning centres differ from the 1-thread rule, both are
     centres of maximal radius covering the voxel, and the oracle's is the smaller in
     (x, y, z) order."""
     from porousmediaanalysis_gb300 import capi
-    exp = "/root/reference/Docs/Example/Expected results from -all"
+    exp = os.path.join(REFERENCE, "Docs", "Example", "Expected results from -all")
     solid = load_example(GOLDEN)
     e, mx, _ = oracle_mod.edt(solid)
     crad2, cx, cy, cz = oracle_mod.containing_balls(e, mx)

@@ -59,3 +59,21 @@ def canonical_throats(labels):
         rank[order] = np.arange(len(uniq), dtype=np.uint32)
         out[sel] = THROAT_MIN + rank[np.searchsorted(uniq, ids)]
     return out.reshape(labels.shape)
+
+
+def rows_digest(x):
+    """Digest of a table's rows (tuples or lists of ints and tuples), independent of whether
+    they came from JSON lists or Python tuples."""
+    import json
+
+    def norm(v):
+        if isinstance(v, (list, tuple)):
+            return [norm(u) for u in v]
+        return int(v)
+    return hashlib.sha256(json.dumps(norm(list(x)), separators=(",", ":")).encode()).hexdigest()
+
+
+def throat_lists_digest(throats):
+    """Digest of a shared-type table without its ids: the sorted (pore list, volume) pairs.
+    Equal for two tables that differ only by a renaming of the ids."""
+    return rows_digest(sorted((tuple(t[2]), t[1]) for t in throats))
