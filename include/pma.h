@@ -323,8 +323,24 @@ int pma_run_folder(pma_ctx* ctx, const char* base_folder, pma_mode mode);
  * [z][x][y]. With out == NULL only dims are filled. */
 int pma_read_tiff_stack(const char* folder, int bytes_per_voxel, pma_dims* dims, void* out,
                         size_t out_bytes);
-/* Writes [z][x][y] voxels as slices 1.tif .. SZ.tif (8-bit grey or 32-bit CMYK LZW). */
+/* Writes [z][x][y] voxels as slices 1.tif .. SZ.tif, zero-padded to the width of SZ so
+ * that the name order is the slice order (8-bit grey or 32-bit CMYK LZW). */
 int pma_write_tiff_stack(const char* folder, int bytes_per_voxel, pma_dims dims, const void* data);
+
+/* The run configuration of a sample folder. Replaces Serializer::ReadConfig
+ * (Serializer.cpp:31-64): the same five lines in the same fscanf format, the resolutions
+ * divided by the smallest one. Unlike the reference, which keeps -1 in fields that do not
+ * parse, a file whose first four lines do not parse, or whose resolutions are not
+ * positive, is rejected with PMA_ERR_IO. */
+typedef struct pma_run_config {
+    double resolution[3];       /* "Resolution of initial images", normalised (smallest = 1) */
+    double max_pore_radius_ratio;
+    int32_t available_memory_mb;
+    int32_t use_d3q7;
+    int32_t threads;            /* -1 when the line is missing */
+    int32_t pad_;
+} pma_run_config;
+int pma_read_config(const char* path, pma_run_config* out);
 
 #ifdef __cplusplus
 }

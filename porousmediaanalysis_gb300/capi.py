@@ -148,6 +148,7 @@ _SIGNATURES = {
     "pma_read_tiff_stack": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(Dims),
                                            ctypes.c_void_p, ctypes.c_size_t]),
     "pma_write_tiff_stack": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, Dims, ctypes.c_void_p]),
+    "pma_read_config": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
 }
 
 _lib = None
@@ -205,8 +206,22 @@ def read_tiff_stack(folder, bytes_per_voxel=1):
     return out
 
 
+class RunConfig(ctypes.Structure):
+    _fields_ = [("resolution", ctypes.c_double * 3), ("max_pore_radius_ratio", ctypes.c_double),
+                ("available_memory_mb", ctypes.c_int32), ("use_d3q7", ctypes.c_int32),
+                ("threads", ctypes.c_int32), ("pad_", ctypes.c_int32)]
+
+
+def read_config(path):
+    """config.txt of a sample folder as a dict (pma_read_config)."""
+    c = RunConfig()
+    check(lib().pma_read_config(str(path).encode(), ctypes.byref(c)))
+    return {"resolution": tuple(c.resolution), "max_pore_radius_ratio": c.max_pore_radius_ratio,
+            "available_memory_mb": c.available_memory_mb, "use_d3q7": c.use_d3q7, "threads": c.threads}
+
+
 def write_tiff_stack(folder, array):
-    """Writes a (SZ, SX, SY) uint8 or 32-bit array as slices 1.tif .. SZ.tif."""
+    """Writes a (SZ, SX, SY) uint8 or 32-bit array as slices 1.tif .. SZ.tif (zero-padded)."""
     import numpy as np
     a = np.ascontiguousarray(array)
     bpv = a.dtype.itemsize

@@ -396,6 +396,19 @@ int pma_read_tiff_stack(const char* folder, int bpv, pma_dims* dims, void* out, 
     });
 }
 
+int pma_read_config(const char* path, pma_run_config* out) {
+    return guarded([&] {
+        PMA_REQUIRE(path && out, PMA_ERR_ARGUMENT, "pma_read_config: null argument");
+        const pma::RunConfig c = pma::read_config(path);
+        std::memset(out, 0, sizeof(*out));
+        for (int i = 0; i < 3; ++i) out->resolution[i] = c.resolution[i];
+        out->max_pore_radius_ratio = c.max_pore_radius_ratio;
+        out->available_memory_mb = c.available_memory_mb;
+        out->use_d3q7 = c.use_d3q7;
+        out->threads = c.threads;
+    });
+}
+
 int pma_write_tiff_stack(const char* folder, int bpv, pma_dims dims, const void* data) {
     return guarded([&] {
         PMA_REQUIRE(folder && data, PMA_ERR_ARGUMENT, "pma_write_tiff_stack: null argument");
@@ -404,7 +417,14 @@ int pma_write_tiff_stack(const char* folder, int bpv, pma_dims dims, const void*
         d.sx = dims.sx;
         d.sy = dims.sy;
         d.sz = dims.sz;
-        pma::write_stack(folder, {}, data, bpv, d);
+        // zero-padded names: the reference (and read_stack) orders slices by name
+        std::vector<std::string> names;
+        const int width = static_cast<int>(std::to_string(std::max(d.sz, 1)).size());
+        for (int z = 0; z < d.sz; ++z) {
+            std::string s = std::to_string(z + 1);
+            names.push_back(std::string(width - s.size(), '0') + s + ".tif");
+        }
+        pma::write_stack(folder, names, data, bpv, d);
     });
 }
 

@@ -53,14 +53,32 @@ def test_watershed_generation_limit(limited_ctx, oracle_mod):
     _still_correct(ctx, oracle_mod)
 
 
+def _u_plateau():
+    """One equal-radius plateau shaped like a U in a 1 x 6 x 5 slice: its two legs start trees
+    of their own in the union-find (each leg's smallest voxel has no smaller equal neighbour),
+    so the bottom bar must union them. Returns (mask, edt2, crad2) for pma_pores."""
+    crad = np.zeros((1, 6, 5), np.uint32)
+    crad[0, :5, 0] = 5
+    crad[0, :5, 4] = 5
+    crad[0, 4, :] = 5
+    mask = np.where(crad > 0, 127, 0).astype(np.uint8)
+    mask[0, 0, 0] = 255
+    return mask, crad.copy(), crad
+
+
 def test_union_find_limit(limited_ctx, oracle_mod):
+    import torch
     import porousmediaanalysis_gb300 as pma
     ctx = limited_ctx
-    vol, _ = make_case("union_small")
+    mask, edt2, crad2 = _u_plateau()
+    dev = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).cuda()
     ctx.set_limits(union_limit=0)
-    _expect_limit(lambda: pma.pipeline_host(ctx, vol, run_geodesic=False, fields=("watershed_labels",)),
-                  "union-find")
+    _expect_limit(lambda: pma.assign_pore_and_throat_ids(ctx, dev(mask), dev(edt2), dev(crad2)), "union-find")
     ctx.set_limits(union_limit=1 << 22)
+    labels, table = pma.assign_pore_and_throat_ids(ctx, dev(mask), dev(edt2), dev(crad2))
+    r = oracle_mod.pores_and_watershed(mask, edt2, crad2, 5)
+    assert (labels.cpu().numpy().view(np.uint32) == r.labels_initial).all()
+    assert table.rows()[0] == r.pores0
     _still_correct(ctx, oracle_mod)
 
 

@@ -112,3 +112,51 @@ def test_package_refuses_to_run_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(capi, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError):
         capi.lib()
+
+
+CONFIG = ("Resolution of initial images: {r}\n"
+          "Available memory in megabytes: 4000\n"
+          "Max ratio of pore radius to seed radius: 2.5\n"
+          "Use D3Q7 stencil: {d}\n"
+          "Number of threads: 7\n")
+
+
+def test_config_reads_the_reference_format(pma_lib, tmp_path):
+    """Serializer.cpp:40-52: five labelled lines; resolutions normalised by the smallest."""
+    from porousmediaanalysis_gb300 import capi
+    p = tmp_path / "config.txt"
+    p.write_text(CONFIG.format(r="1 1 1", d=0))
+    c = capi.read_config(p)
+    assert c == {"resolution": (1.0, 1.0, 1.0), "max_pore_radius_ratio": 2.5, "available_memory_mb": 4000,
+                 "use_d3q7": 0, "threads": 7}
+    p.write_text(CONFIG.format(r="2 3 4", d=1).replace("\n", "\r\n"))  # Windows line ends
+    c = capi.read_config(p)
+    assert c["resolution"] == (1.0, 1.5, 2.0) and c["use_d3q7"] == 1 and c["threads"] == 7
+
+
+@pytest.mark.parametrize("text", [
+    "",
+    "Resolution of initial images: 1 1\nAvailable memory in megabytes: 4000\n",
+    CONFIG.format(r="1 1 1", d=0).replace("Available memory", "Memory"),
+    CONFIG.format(r="0 1 1", d=0),
+    CONFIG.format(r="1 -1 1", d=0),
+])
+def test_config_rejects_malformed_files(pma_lib, tmp_path, text):
+    from porousmediaanalysis_gb300 import capi
+    p = tmp_path / "config.txt"
+    p.write_text(text)
+    with pytest.raises(capi.PmaError) as e:
+        capi.read_config(p)
+    assert e.value.status == 3  # PMA_ERR_IO
+    with pytest.raises(capi.PmaError):
+        capi.read_config(tmp_path / "missing.txt")
+
+
+def test_written_stack_keeps_slice_order(pma_lib, tmp_path):
+    """Slices are named with zero padding, so the name order (by which the reference and the
+    reader sort) is the slice order beyond nine slices."""
+    from porousmediaanalysis_gb300 import capi
+    a = np.arange(12 * 3 * 4, dtype=np.uint8).reshape(12, 3, 4)
+    capi.write_tiff_stack(str(tmp_path / "s"), a)
+    assert sorted(os.listdir(tmp_path / "s"))[:3] == ["01.tif", "02.tif", "03.tif"]
+    assert np.array_equal(capi.read_tiff_stack(str(tmp_path / "s"), 1), a)
