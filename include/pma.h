@@ -77,6 +77,10 @@ typedef struct pma_limits {
 } pma_limits;
 int pma_ctx_get_limits(const pma_ctx* ctx, pma_limits* out);
 int pma_ctx_set_limits(pma_ctx* ctx, const pma_limits* limits);
+/* Shared-type numbering of pma_pores: 1 (default) the reference's creation order, 0 a
+ * cheaper order that matches it up to a renaming. Batch and server lanes created later
+ * inherit it. */
+int pma_ctx_set_throat_numbering(pma_ctx* ctx, int reference_order);
 /* Runs one bounded device wait on a flag that nothing sets (the watershed's frontier
  * look-back waiting for a chunk that never publishes), with the context's spin_limit. Sets
  * *timed_out = 1 when the wait gave up and reported it, as it must. No counterpart in the
@@ -163,9 +167,13 @@ void pma_table_free(pma_table* t);
  * PoreAndThroatComputer::AssignPoreAndThroatIds (PoreAndThroatComputer.cpp:35-55; seeds
  * :93-163, propagation :192-269, pixel states BasePoreAndThroatComputer.cpp:37-133).
  * Pore ids, seeds, radii, volumes, boundary flags and every voxel's pore set are exact.
- * Throat ids count down from UINT32_MAX - 1 in order of (last pore of the throat, first
- * voxel of the throat); the reference numbers them in its depth-first creation order, so
- * throat ids match it up to a one-to-one renaming.
+ * Shared-type ("throat") ids are the reference's: they count down from UINT32_MAX - 1 in
+ * the order the reference's depth-first searches create the types (types deleted later
+ * included), which a host replay of each pore's search order reproduces. With
+ * pma_ctx_set_throat_numbering(ctx, 0) the replay is skipped and the ids count down in
+ * order of (last pore of the type, first voxel of the type) instead: the same types, the
+ * same labels up to a one-to-one renaming of the type ids. Nothing downstream of the
+ * empty-pore removal depends on the numbering (the watershed reads only the pores).
  * d_labels is written completely. */
 int pma_pores(pma_ctx* ctx, const uint8_t* d_maxball_mask, const uint32_t* d_edt2,
               const uint32_t* d_crad2, pma_dims dims, pma_stencil stencil, uint32_t* d_labels,

@@ -90,6 +90,11 @@ class Context:
         lim = capi.Limits(**cur)
         capi.check(capi.lib().pma_ctx_set_limits(self.handle, ctypes.byref(lim)))
 
+    def set_throat_numbering(self, reference=True):
+        """Shared-type ids of the initial propagation: the reference's creation order (default),
+        or a cheaper order equal to it up to a renaming (pma_ctx_set_throat_numbering)."""
+        capi.check(capi.lib().pma_ctx_set_throat_numbering(self.handle, int(bool(reference))))
+
     def selftest_bounded_wait(self):
         """True when a device wait on a flag nothing sets gave up after spin_limit polls and
         reported it (pma_selftest_bounded_wait)."""

@@ -15,8 +15,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
-LIB_SOURCES = ["capi.cpp", "pipeline.cpp", "batch.cpp", "serve.cpp", "pma_io.cpp", "edt.cu", "balls.cu", "geodesic.cu",
-               "pores.cu", "watershed.cu"]
+LIB_SOURCES = ["capi.cpp", "pipeline.cpp", "batch.cpp", "serve.cpp", "pma_io.cpp", "exact_ids.cpp", "edt.cu",
+               "balls.cu", "geodesic.cu", "pores.cu", "watershed.cu", "resample.cu"]
 LIB = os.path.join(OUT, "libpma.so")
 CLI = os.path.join(OUT, "pma")
 

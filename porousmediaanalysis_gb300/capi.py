@@ -103,6 +103,7 @@ _SIGNATURES = {
     "pma_ctx_get_limits": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Limits)]),
     "pma_ctx_set_limits": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Limits)]),
     "pma_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "pma_ctx_set_throat_numbering": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "pma_edt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, Dims, ctypes.c_void_p,
                                ctypes.POINTER(EdtStats), ctypes.c_void_p, ctypes.c_size_t]),
     "pma_pipeline_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_size_t,

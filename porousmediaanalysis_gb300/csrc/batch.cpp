@@ -30,6 +30,7 @@ pma_ctx* make_lane(const pma_ctx* parent) {
     c->smem_optin = parent->smem_optin;
     c->timing = false;
     c->limits = parent->limits;
+    c->reference_throat_ids = parent->reference_throat_ids;
     const cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;

@@ -203,6 +203,13 @@ int pma_ctx_set_limits(pma_ctx* ctx, const pma_limits* limits) {
     });
 }
 
+int pma_ctx_set_throat_numbering(pma_ctx* ctx, int reference_order) {
+    return guarded([&] {
+        PMA_REQUIRE(ctx, PMA_ERR_ARGUMENT, "pma_ctx_set_throat_numbering: null context");
+        ctx->reference_throat_ids = reference_order != 0;
+    });
+}
+
 int pma_selftest_bounded_wait(pma_ctx* ctx, int* timed_out) {
     return guarded([&] {
         PMA_REQUIRE(ctx && timed_out, PMA_ERR_ARGUMENT, "pma_selftest_bounded_wait: null argument");

@@ -2,6 +2,7 @@
 // reference's command-line modes (CommandLineDispatcher.cpp:34-72,
 // ImageProcessingManager.cpp:63-108).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -333,6 +334,91 @@ void write_cavities(const Folder& f, const pma_cavity* c, int n) {  // Serialize
     std::fclose(o);
 }
 
+std::string file_name(const std::string& path) {
+    const size_t s = path.find_last_of('/');
+    return s == std::string::npos ? path : path.substr(s + 1);
+}
+
+void copy_file(const std::string& from, const std::string& to) {
+    FILE* i = std::fopen(from.c_str(), "rb");
+    PMA_REQUIRE(i, PMA_ERR_IO, "cannot open " + from);
+    FILE* o = std::fopen(to.c_str(), "wb");
+    if (!o) {
+        std::fclose(i);
+        throw Error(PMA_ERR_IO, "cannot write " + to);
+    }
+    char b[1 << 16];
+    size_t k;
+    bool ok = true;
+    while ((k = std::fread(b, 1, sizeof(b), i)) > 0) ok = ok && std::fwrite(b, 1, k, o) == k;
+    std::fclose(i);
+    ok = (std::fclose(o) == 0) && ok;
+    PMA_REQUIRE(ok, PMA_ERR_IO, "cannot write " + to);
+}
+
+// ImageResampler::ResampleImages (ImageResampler.cpp:28-67): when the configured resolution
+// makes the image size differ from the slices', the slices move to Original/ and Images/
+// receives the resampled ones: slice i of the new stack copies original slice
+// (int)(i / resolution_z) (repeated names get "_1", "_2", ... before the extension,
+// :184-207), and, when the in-plane size changes too, each is upsampled in plane
+// (resample.cu). Runs once: an existing Original/ folder means it already ran.
+void resample_images(pma_ctx* ctx, const std::string& base, const RunConfig& cfg) {
+    const std::string images = join(base, kImages), original = join(base, "Original");
+    if (path_exists(original)) return;
+    const std::vector<std::string> paths = list_tiff_stack(images);
+    PMA_REQUIRE(!paths.empty(), PMA_ERR_IO,
+                "Initial images folder, \"Images\", which shall be near the config.txt file, is empty: " + base);
+    const TiffImage first = read_tiff(paths[0]);
+    const int actual[3] = {first.rows, first.cols, static_cast<int>(paths.size())};
+    int target[3];
+    for (int a = 0; a < 3; ++a)  // Serializer.cpp:247-251 (Math::Round)
+        target[a] = static_cast<int>(std::floor(actual[a] * cfg.resolution[a] + 0.5));
+    if (target[0] == actual[0] && target[1] == actual[1] && target[2] == actual[2]) return;
+    PMA_REQUIRE(std::rename(images.c_str(), original.c_str()) == 0, PMA_ERR_IO, "cannot rename " + images);
+    ensure_dir(images);
+    const std::vector<std::string> before = list_tiff_stack(original);
+    std::vector<int> source(target[2]);
+    std::vector<std::string> names(target[2]);
+    std::string previous;
+    int dup = 0;
+    for (int i = 0; i < target[2]; ++i) {  // :209-218, :184-207
+        source[i] = static_cast<int>(i / cfg.resolution[2]);
+        PMA_REQUIRE(source[i] < static_cast<int>(before.size()), PMA_ERR_INTERNAL, "resample: slice index");
+        std::string name = file_name(before[source[i]]);
+        if (name == previous) {
+            ++dup;
+            const size_t dot = name.find_last_of('.');
+            name = name.substr(0, dot) + "_" + std::to_string(dup) + name.substr(dot);
+        } else {
+            dup = 0;
+            previous = name;
+        }
+        names[i] = name;
+        copy_file(before[source[i]], join(images, name));  // :152-160
+    }
+    if (target[0] == actual[0] && target[1] == actual[1]) return;
+    // in-plane upsampling of every original slice, written under each of its names
+    const size_t plane = static_cast<size_t>(actual[0]) * actual[1];
+    std::vector<uint8_t> src(plane * before.size());
+    for (size_t k = 0; k < before.size(); ++k) {
+        const TiffImage im = read_tiff(before[k]);
+        PMA_REQUIRE(im.rows == actual[0] && im.cols == actual[1] && im.bits == 8, PMA_ERR_IO,
+                    "Image size is incorrect in " + before[k]);
+        std::memcpy(src.data() + k * plane, im.data.data(), plane);
+    }
+    const std::vector<uint8_t> out = resample_slices(ctx, src, static_cast<int>(before.size()), actual[0],
+                                                     actual[1], target[0], target[1]);
+    const size_t plane2 = static_cast<size_t>(target[0]) * target[1];
+    for (int i = 0; i < target[2]; ++i) {
+        TiffImage im;
+        im.rows = target[0];
+        im.cols = target[1];
+        im.bits = 8;
+        im.data.assign(out.begin() + source[i] * plane2, out.begin() + (source[i] + 1) * plane2);
+        write_tiff(join(images, names[i]), im);
+    }
+}
+
 struct TableGuard {
     pma_table* t = nullptr;
     ~TableGuard() { delete t; }
@@ -342,9 +428,8 @@ void run_one(pma_ctx* ctx, const std::string& base, pma_mode mode) {
     Folder f;
     f.base = base;
     f.cfg = read_config(join(base, "config.txt"));
-    PMA_REQUIRE(f.cfg.resolution[0] == 1 && f.cfg.resolution[1] == 1 && f.cfg.resolution[2] == 1,
-                PMA_ERR_ARGUMENT,
-                "only \"Resolution of initial images: 1 1 1\" is supported (no resampling) in " + base);
+    // -edt (and -all) and -spd resample first (ImageProcessingManager.cpp:76-80, 101-105)
+    if (mode == PMA_MODE_ALL || mode == PMA_MODE_EDT || mode == PMA_MODE_SPD) resample_images(ctx, base, f.cfg);
     std::vector<std::string> slices = list_tiff_stack(join(base, kImages));
     PMA_REQUIRE(!slices.empty(), PMA_ERR_IO,
                 "Initial images folder, \"Images\", which shall be near the config.txt file, is empty: " + base);

@@ -86,6 +86,7 @@ struct pma_ctx {
     std::vector<Timed> timed;
     std::vector<pma_ctx*> lanes;  // child contexts of batch calls (own stream and scratch)
     pma_limits limits{1 << 20, 1 << 22, (1ull << 23) - 1, 0};  // device loop bounds
+    bool reference_throat_ids = true;  // pma_pores numbers shared types as the reference does
     // Demand: the largest size each named buffer was asked for since reset_demand(), summed;
     // what one request needs, whatever earlier requests left in the cache.
     std::map<std::string, size_t> demand;
@@ -162,6 +163,15 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
 pma_table* watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* crad2, pma_dims d,
                      pma_stencil st, uint32_t max_edt2, uint32_t* labels);
 void wait_selftest(pma_ctx* ctx, int* timed_out);
+// resample.cu: 8-bit slices [nz][sx][sy] (host) upsampled in plane to [nz][dx][dy] as the
+// reference's image rescale does.
+std::vector<uint8_t> resample_slices(pma_ctx* ctx, const std::vector<uint8_t>& src, int nz, int sx, int sy, int dx,
+                                     int dy);
+// exact_ids.cpp: the reference's shared-type ids of the initial propagation, per type row.
+std::vector<uint32_t> replay_type_ids(const uint32_t* crad, const uint32_t* labels, pma_dims d, bool d3q7,
+                                      const std::vector<pma_pore>& pores,
+                                      const std::vector<std::vector<uint32_t>>& lists,
+                                      const std::vector<uint32_t>& fast_ids);
 
 // Copies the first `cap` cavity rows to `out` and reports how many there are in all.
 inline void copy_cavities(const std::vector<pma_cavity>& rows, pma_cavity* out, int cap, int* n) {

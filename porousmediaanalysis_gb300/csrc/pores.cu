@@ -22,9 +22,9 @@
 //  * A voxel's label is its seed's pore id when |S| = 1 and a shared type ("throat") when
 //    |S| >= 2. Pore volumes, boundary flags, type volumes and type pore lists are exact.
 //    The reference numbers types in its depth-first creation order, which also consumed ids
-//    for types deleted later; here the surviving types are numbered by (last pore of the
-//    type, first voxel of the type), so type ids match the reference up to a one-to-one
-//    renaming.
+//    for types deleted later. The types are first numbered by (last pore of the type, first
+//    voxel of the type), then renumbered in the reference's order by a host replay of each
+//    pore's search order (exact_ids.cpp), unless the context asks for the cheaper numbering.
 #include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
@@ -1049,6 +1049,9 @@ T* buf(pma_ctx* ctx, const char* tag, size_t count) {
 
 }  // namespace
 
+void reference_type_ids(pma_ctx* ctx, pma_table* t, uint32_t* labels, const uint32_t* crad2, pma_dims d,
+                        pma_stencil st);
+
 pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const uint32_t* crad2,
                  pma_dims d, pma_stencil st, uint32_t* labels) {
     KernelTimer kt_stage(ctx, "stage_pores");  // the whole stage, for the untimed remainder
@@ -1158,9 +1161,13 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         ctx->check_launch("scatter_pid");
         to_pid<<<G, 256, 0, s>>>(labels, n, np, pid, err);
         ctx->check_launch("to_pid");
+    }
+    {
+        // the union-find's own bound (bit 1) is read here: the level sweep reuses the word
         unsigned int h_err = 0;
         PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
         ctx->sync();
+        PMA_REQUIRE(!(h_err & 1u), PMA_ERR_LIMIT, "pma_pores: plateau union-find did not converge");
         PMA_REQUIRE(!(h_err & 8u), PMA_ERR_INTERNAL, "pma_pores: plateau labelling left a non-root parent");
     }
     kt_ids.reset();
@@ -1397,7 +1404,6 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
         PMA_CUDA(cudaMemcpyAsync(&used, base, 8, cudaMemcpyDeviceToHost, s));
         ctx->sync();
-        PMA_REQUIRE(!(h_err & 1u), PMA_ERR_LIMIT, "pma_pores: plateau union-find did not converge");
         PMA_REQUIRE(!(h_err & 32u), PMA_ERR_INTERNAL, "pma_pores: merged seed sets disagree with their bounds");
         if (!(h_err & 2u)) break;
         PMA_REQUIRE(attempt < 2, PMA_ERR_MEMORY, "pma_pores: seed-set pool overflow");
@@ -1605,7 +1611,66 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         t->pool[at++] = L[0];
         for (size_t j = 2; j < nl; ++j) t->pool[at++] = L[j];
     }
+    if (ctx->reference_throat_ids && ngroups) {
+        KernelTimer kt_exact(ctx, "exact_type_ids");
+        reference_type_ids(ctx, t, labels, crad2, d, st);
+    }
     return t;
+}
+
+// Renumbers the shared types of the initial propagation in the reference's creation order
+// (exact_ids.cpp) and relabels their voxels.
+void reference_type_ids(pma_ctx* ctx, pma_table* t, uint32_t* labels, const uint32_t* crad2, pma_dims d,
+                        pma_stencil st) {
+    cudaStream_t s = ctx->stream;
+    const size_t n = voxels(d);
+    const size_t ng = t->throats.size();
+    std::vector<uint32_t> h_labels(n), h_crad(n);
+    PMA_CUDA(cudaMemcpyAsync(h_labels.data(), labels, n * 4, cudaMemcpyDeviceToHost, s));
+    PMA_CUDA(cudaMemcpyAsync(h_crad.data(), crad2, n * 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    std::vector<std::vector<uint32_t>> lists(ng);
+    std::vector<uint32_t> fast(ng);
+    for (size_t g = 0; g < ng; ++g) {
+        const pma_throat& th = t->throats[g];
+        lists[g].assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
+        std::sort(lists[g].begin(), lists[g].end());
+        fast[g] = th.id;
+    }
+    const std::vector<uint32_t> exact =
+        replay_type_ids(h_crad.data(), h_labels.data(), d, st == PMA_D3Q7, t->pores, lists, fast);
+    // voxels: old id -> new id (old ids ascending, as the rows are)
+    std::vector<uint32_t> old_ids(ng), new_ids(ng);
+    for (size_t g = 0; g < ng; ++g) {
+        old_ids[g] = fast[g];
+        new_ids[g] = exact[g];
+    }
+    PMA_REQUIRE(std::is_sorted(old_ids.begin(), old_ids.end()), PMA_ERR_INTERNAL, "pma_pores: type rows out of order");
+    uint32_t* d_old = buf<uint32_t>(ctx, "pores.exact_old", ng);
+    uint32_t* d_new = buf<uint32_t>(ctx, "pores.exact_new", ng);
+    PMA_CUDA(cudaMemcpyAsync(d_old, old_ids.data(), ng * 4, cudaMemcpyHostToDevice, s));
+    PMA_CUDA(cudaMemcpyAsync(d_new, new_ids.data(), ng * 4, cudaMemcpyHostToDevice, s));
+    remap_labels<<<grid_for(ctx, n), 256, 0, s>>>(labels, n, d_old, d_new, static_cast<uint32_t>(ng));
+    ctx->check_launch("remap_labels");
+    // rows in ascending (new) id order
+    std::vector<size_t> order(ng);
+    for (size_t g = 0; g < ng; ++g) order[g] = g;
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return exact[a] < exact[b]; });
+    std::vector<pma_throat> rows;
+    std::vector<uint32_t> pool;
+    rows.reserve(ng);
+    pool.reserve(t->pool.size());
+    for (size_t k = 0; k < ng; ++k) {
+        pma_throat th = t->throats[order[k]];
+        const uint64_t off = th.pool_offset;
+        th.id = exact[order[k]];
+        th.pool_offset = pool.size();
+        pool.insert(pool.end(), t->pool.begin() + off, t->pool.begin() + off + th.n_pores);
+        rows.push_back(th);
+    }
+    t->throats.swap(rows);
+    t->pool.swap(pool);
+    ctx->sync();
 }
 
 // a11: EmptyPoresRemover.cpp:31-244 on the host table, then one relabel launch.

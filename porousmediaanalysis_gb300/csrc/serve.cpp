@@ -190,6 +190,7 @@ int pma_server_create(pma_ctx* ctx, const pma_server_config* cfg, pma_server** o
                             "pma_server_create: lane context");
                 c->blocking_sync = true;
                 c->limits = ctx->limits;
+                c->reference_throat_ids = ctx->reference_throat_ids;
                 l.ctx = c;
             }
         } catch (...) {

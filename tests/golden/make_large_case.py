@@ -43,9 +43,13 @@ def main():
         "maximum_balls_count": int(o["maximum_balls_count"]),
         "pores0": [list(p) for p in r.pores0],
         "throats0_lists": sorted([[t[2], t[1]] for t in r.throats0]),
+        "throats0": [[t[0], t[1], list(t[2])] for t in r.throats0],
         "labels_initial_canonical": digest(canonical_throats(r.labels_initial)),
+        "labels_initial": digest(r.labels_initial),
         "pores": [list(p) for p in r.pores],
+        "throats": [[t[0], t[1], list(t[2])] for t in r.throats],
         "labels_canonical": digest(canonical_throats(r.labels)),
+        "labels": digest(r.labels),
         "labels_ws": digest(r.labels_ws),
         "pores_ws": [list(p) for p in r.pores_ws],
         "throats_ws": [list(t) for t in r.throats_ws],

@@ -3,9 +3,7 @@ config.txt and Images/ is processed like the reference's `-all` and `-spd` modes
 (CommandLineDispatcher.cpp:34-72), and every file it writes is compared with the reference
 run with one thread on the same volume: text files byte for byte
 (tests/golden/folder_texts.json, made by tests/golden/make_folder_texts.py), TIFF folders as
-decoded fields against the reference's digests. The shared-type ids of sharedPixelTypes.txt
-and PoreThroatIds, which the reference numbers in its depth-first creation order, are
-compared up to a renaming.
+decoded fields against the reference's digests, shared-type ids included.
 """
 import json
 import os
@@ -16,15 +14,16 @@ import pytest
 
 from cases import load_example, make_case, many_pockets
 from conftest import GOLDEN, ROOT
-from util import canonical_throats, digest
+from util import digest
 
 pytestmark = pytest.mark.gpu
 
 EXACT_TEXTS = ("intermediateStatistics.txt", "euclideanDistanceSquareCounts.txt", "pores.txt",
-               "poresWatershed.txt", "sharedPixelTypesWatershed.txt", "cavityDescriptions.txt")
+               "sharedPixelTypes.txt", "poresWatershed.txt", "sharedPixelTypesWatershed.txt",
+               "cavityDescriptions.txt")
 FOLDERS = {"EuclideanDistanceSquares": 4, "ContainingBallRadiiSquares": 4, "ContainingBallCoordinatesX": 4,
            "ContainingBallCoordinatesY": 4, "ContainingBallCoordinatesZ": 4, "IsMaximumBall": 1,
-           "PoreThroatIdsWatershed": 4, "ShortestPathDistances": 4, "CavityIds": 4}
+           "PoreThroatIds": 4, "PoreThroatIdsWatershed": 4, "ShortestPathDistances": 4, "CavityIds": 4}
 
 
 @pytest.fixture(scope="module")
@@ -47,26 +46,14 @@ def make_sample(root, vol, d3q7=False, resolution="1 1 1"):
     return sample
 
 
-def _throat_lists(text):
-    rows = []
-    for line in text.strip().splitlines()[1:]:
-        tid, vol, rest = line.split(";", 2)
-        rows.append((tuple(int(x) for x in rest.split()), int(vol)))
-    return sorted(rows)
-
-
 def check_sample(sample, ref_texts, rec):
     from porousmediaanalysis_gb300 import capi
     for name in EXACT_TEXTS:
         with open(os.path.join(sample, name)) as f:
             assert f.read() == ref_texts[name], name
-    with open(os.path.join(sample, "sharedPixelTypes.txt")) as f:
-        assert _throat_lists(f.read()) == _throat_lists(ref_texts["sharedPixelTypes.txt"])
     for name, bpv in FOLDERS.items():
         a = capi.read_tiff_stack(os.path.join(sample, name), bpv)
         assert digest(a) == rec["digests"][name], name
-    p = capi.read_tiff_stack(os.path.join(sample, "PoreThroatIds"), 4)
-    assert digest(canonical_throats(p)) == rec["PoreThroatIds_canonical"]
 
 
 @pytest.mark.parametrize("name", ["two_cavities", "pack_small", "union_small_d3q7", "slab_rows"])
