@@ -472,8 +472,11 @@ def main():
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # whole-stage regions (stage_*) bracket the kernels; the dominant one is a kernel region
-    kk = {k: v for k, v in kern.items() if not k.startswith("stage_")}
+    # the dominant region among the kernels whose algorithmic bytes are stated (whole-stage
+    # regions stage_* and host-side regions bracket several kernels; count.* are work counters)
+    counters = {k[len("count."):]: v[0] / args.steps for k, v in kern.items() if k.startswith("count.")}
+    kern = {k: v for k, v in kern.items() if not k.startswith("count.")}
+    kk = {k: v for k, v in kern.items() if k in ALGO_BYTES}
     dom = max(kk.items(), key=lambda kv: kv[1][0]) if kk else ("none", (0.0, 1))
     name, (tot_ms, nlaunch) = dom
     per_launch_ms = tot_ms / max(nlaunch, 1)
@@ -489,7 +492,8 @@ def main():
                 "traffic_unit": "bytes per launch", "traffic_source": traffic_src,
                 "algorithmic_bytes_per_launch": algo,
                 "kernel_ms_per_step": tot_ms / args.steps,
-                "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(kern.items())}}
+                "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(kern.items())},
+                "counters_per_step": counters}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

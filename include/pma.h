@@ -62,7 +62,8 @@ uint64_t pma_ctx_launch_count(const pma_ctx* ctx);
 /* Opt-in kernel timing: with timing on, the hot kernels are bracketed by CUDA events on
  * the context's stream. The report is a JSON object {"kernel": [total_ms, launches], ...}
  * of everything timed since the previous report; each call consumes the timed events, so
- * pass a buffer large enough for the whole report. Returns its full length. */
+ * pass a buffer large enough for the whole report. Returns its full length. Work counters
+ * of the timed calls appear as "count.<name>": [sum, increments]. */
 int pma_ctx_set_timing(pma_ctx* ctx, int enable);
 size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap);
 /* Bounds of the data-dependent device loops. Each loop that reaches its bound stops and the
@@ -77,9 +78,9 @@ typedef struct pma_limits {
 } pma_limits;
 int pma_ctx_get_limits(const pma_ctx* ctx, pma_limits* out);
 int pma_ctx_set_limits(pma_ctx* ctx, const pma_limits* limits);
-/* Shared-type numbering of pma_pores: 1 (default) the reference's creation order, 0 a
- * cheaper order that matches it up to a renaming. Batch and server lanes created later
- * inherit it. */
+/* Shared-type numbering of pma_pores: 0 (default) an order that matches the reference's up
+ * to a renaming, 1 the reference's creation order (a host replay; see pma_pores). Batch and
+ * server lanes created later inherit it. pma_run_folder always uses the reference's. */
 int pma_ctx_set_throat_numbering(pma_ctx* ctx, int reference_order);
 /* Runs one bounded device wait on a flag that nothing sets (the watershed's frontier
  * look-back waiting for a chunk that never publishes), with the context's spin_limit. Sets
@@ -167,14 +168,17 @@ void pma_table_free(pma_table* t);
  * PoreAndThroatComputer::AssignPoreAndThroatIds (PoreAndThroatComputer.cpp:35-55; seeds
  * :93-163, propagation :192-269, pixel states BasePoreAndThroatComputer.cpp:37-133).
  * Pore ids, seeds, radii, volumes, boundary flags and every voxel's pore set are exact.
- * Shared-type ("throat") ids are the reference's: they count down from UINT32_MAX - 1 in
- * the order the reference's depth-first searches create the types (types deleted later
- * included), which a host replay of each pore's search order reproduces. With
- * pma_ctx_set_throat_numbering(ctx, 0) the replay is skipped and the ids count down in
- * order of (last pore of the type, first voxel of the type) instead: the same types, the
- * same labels up to a one-to-one renaming of the type ids. Nothing downstream of the
- * empty-pore removal depends on the numbering (the watershed reads only the pores).
- * d_labels is written completely. */
+ * Shared-type ("throat") ids count down from UINT32_MAX - 1. By default they are numbered
+ * in order of (last pore of the type, first voxel of the type): the reference's types and
+ * labels up to a one-to-one renaming of the type ids. After
+ * pma_ctx_set_throat_numbering(ctx, 1) they are the reference's own ids: the order in which
+ * its depth-first searches create the types (types deleted later included), reproduced by
+ * a host replay of each pore's search order. That replay is sequential per pore and costs
+ * about one visit per voxel of every pore's reach set (tens of seconds at 1024^3), so the
+ * folder-level entry point uses it (it writes these ids into PoreThroatIds and
+ * sharedPixelTypes.txt) and the other entry points leave it to the caller. Nothing
+ * downstream of the empty-pore removal depends on the numbering (the watershed reads only
+ * the pores). d_labels is written completely. */
 int pma_pores(pma_ctx* ctx, const uint8_t* d_maxball_mask, const uint32_t* d_edt2,
               const uint32_t* d_crad2, pma_dims dims, pma_stencil stencil, uint32_t* d_labels,
               pma_table** out);

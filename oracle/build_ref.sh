@@ -1,6 +1,7 @@
 #!/bin/sh
 # Compiles the reference's own C++ sources (where they lie, read-only) into the checker
-# binary oracle/_ref/pma_ref, with oracle/ref_shim standing in for FreeImage. Test
+# binary oracle/_ref/pma_ref, with oracle/ref_shim standing in for FreeImage's file I/O and
+# FreeImage's own resize engine (Resize.cpp, Rescale.cpp) compiled over a minimal bitmap. Test
 # infrastructure only; needs the reference tree: the first argument, else $PMA_REFERENCE_DIR,
 # else /root/reference.
 set -e
@@ -16,6 +17,13 @@ for s in $SRCS; do
   g++ $CXXFLAGS -include sys/types.h -c "$s" -o "$o" &
   pids="$pids $!"
 done
-for p in $pids; do wait $p; done
+# FreeImage's resize engine, from the reference's vendored sources, for the in-plane resampling
+FI="$REF/Externals/FreeImage/Source"
+FIFLAGS="-O2 -w -ffp-contract=off -I$FI -I$FI/FreeImageToolkit"
+for s in "$FI/FreeImageToolkit/Resize.cpp" "$FI/FreeImageToolkit/Rescale.cpp" "$HERE/ref_shim/fi_resize_shim.cpp"; do
+  g++ $FIFLAGS -c "$s" -o "$OUT/obj/fi_$(basename "$s" .cpp).o" &
+  pids="$pids $!"
+done
+for p in $pids; do wait $p || exit 1; done
 g++ -fopenmp "$OUT"/obj/*.o -o "$OUT/pma_ref"
 echo "$OUT/pma_ref"

@@ -48,8 +48,9 @@ def read_stack(folder, dtype):
     return np.stack([_read_slice(os.path.join(folder, n), dtype) for n in names])
 
 
-def run(solid, modes=("-all", "-spd"), threads=1, d3q7=False, keep=None):
-    """solid: (SZ, SX, SY) array, non-zero = solid. Returns (fields dict, text files dict)."""
+def run(solid, modes=("-all", "-spd"), threads=1, d3q7=False, keep=None, resolution="1 1 1"):
+    """solid: (SZ, SX, SY) array, non-zero = solid. Returns (fields dict, text files dict);
+    fields include "Images", the (possibly resampled) input stack after the run."""
     assert os.path.exists(REF_BIN), "build the reference checker with oracle/build_ref.sh"
     root = keep or tempfile.mkdtemp(prefix="pma_ref_")
     sample = os.path.join(root, "sample")
@@ -60,16 +61,16 @@ def run(solid, modes=("-all", "-spd"), threads=1, d3q7=False, keep=None):
         _write_slice(os.path.join(sample, "Images", "%0*d.tif" % (width, z + 1)),
                      np.where(np.asarray(solid[z]) != 0, 255, 0).astype(np.uint8))
     with open(os.path.join(sample, "config.txt"), "w") as f:
-        f.write("Resolution of initial images: 1 1 1\n"
+        f.write("Resolution of initial images: %s\n"
                 "Available memory in megabytes: 200000\n"
                 "Max ratio of pore radius to seed radius: 10.0\n"
                 "Use D3Q7 stencil: %d\n"
-                "Number of threads: %d\n" % (1 if d3q7 else 0, threads))
+                "Number of threads: %d\n" % (resolution, 1 if d3q7 else 0, threads))
     for m in modes:
         r = subprocess.run([REF_BIN, m], cwd=root, capture_output=True, text=True)
         if r.returncode != 0 or "rror" in r.stdout[-300:]:
             raise RuntimeError("reference failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
-    fields = {}
+    fields = {"Images": read_stack(os.path.join(sample, "Images"), np.uint8)}
     for name, dt in FIELDS.items():
         p = os.path.join(sample, name)
         if os.path.isdir(p):

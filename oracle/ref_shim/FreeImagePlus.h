@@ -22,6 +22,9 @@
 #define FILTER_BILINEAR 2
 #define FIT_RGBA16 10
 
+extern "C" int pma_shim_rescale8(const unsigned char* bits, unsigned w, unsigned h, unsigned nw, unsigned nh,
+                                 unsigned char* out);
+
 class fipImage {
   public:
     fipImage() : width_(0), height_(0), bpp_(0) {}
@@ -76,7 +79,17 @@ class fipImage {
     bool convertTo32Bits() { return setBpp(32); }
     bool convertToType(int, bool) { return setBpp(64); }
 
+    // FreeImage's own bilinear rescale for 8-bit images (its Resize.cpp compiled with
+    // fi_resize_shim.cpp); other sizes are only reallocated, as their pixels are overwritten.
     bool rescale(unsigned w, unsigned h, int) {
+        if (bpp_ == 8 && width_ && height_) {
+            std::vector<BYTE> out(static_cast<size_t>(w) * h);
+            if (pma_shim_rescale8(&bits_[0], width_, height_, w, h, &out[0]) != 0) return false;
+            width_ = w;
+            height_ = h;
+            bits_.swap(out);
+            return true;
+        }
         width_ = w;
         height_ = h;
         bits_.assign(static_cast<size_t>(getScanWidth()) * height_, 0);

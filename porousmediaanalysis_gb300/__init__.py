@@ -91,8 +91,9 @@ class Context:
         capi.check(capi.lib().pma_ctx_set_limits(self.handle, ctypes.byref(lim)))
 
     def set_throat_numbering(self, reference=True):
-        """Shared-type ids of the initial propagation: the reference's creation order (default),
-        or a cheaper order equal to it up to a renaming (pma_ctx_set_throat_numbering)."""
+        """Shared-type ids of the initial propagation: the reference's creation order (a host
+        replay), or the default cheaper order equal to it up to a renaming
+        (pma_ctx_set_throat_numbering)."""
         capi.check(capi.lib().pma_ctx_set_throat_numbering(self.handle, int(bool(reference))))
 
     def selftest_bounded_wait(self):

@@ -241,6 +241,8 @@ size_t pma_ctx_timing_report(pma_ctx* ctx, char* buf, size_t cap) {
             cudaEventDestroy(t.stop);
         }
         ctx->timed.clear();
+        for (auto& kv : ctx->counters) acc["count." + kv.first] = kv.second;
+        ctx->counters.clear();
         bool first = true;
         char item[256];
         for (auto& kv : acc) {

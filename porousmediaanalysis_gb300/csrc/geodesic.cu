@@ -397,6 +397,7 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
             rb.add(h, misc, 5 * 8);
             read_back(ctx, rb);
         }
+        ctx->count("geo.buckets", k);
         const unsigned walls_bits = static_cast<unsigned>(h[3]);
         const unsigned long long settled = h[4];
         const int reached = __builtin_popcount(walls_bits);

@@ -527,6 +527,15 @@ extern "C" int pma_run_folder(pma_ctx* ctx, const char* base_folder, pma_mode mo
                     "pma_run_folder: unknown mode");
         PMA_CUDA(cudaSetDevice(ctx->device));
         std::vector<std::string> folders = pma::folders_with(base_folder, "config.txt");
-        for (const std::string& f : folders) pma::run_one(ctx, f, mode);
+        // the files written hold the shared-type ids, so they are numbered as the reference does
+        const bool numbering = ctx->reference_throat_ids;
+        ctx->reference_throat_ids = true;
+        try {
+            for (const std::string& f : folders) pma::run_one(ctx, f, mode);
+        } catch (...) {
+            ctx->reference_throat_ids = numbering;
+            throw;
+        }
+        ctx->reference_throat_ids = numbering;
     });
 }

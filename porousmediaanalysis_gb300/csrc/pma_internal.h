@@ -84,9 +84,17 @@ struct pma_ctx {
         cudaEvent_t start, stop;
     };
     std::vector<Timed> timed;
+    // Work counters of the timed calls (reported with the timings as [sum, increments]).
+    std::map<std::string, std::pair<double, long long>> counters;
+    void count(const std::string& name, double v) {
+        if (!timing) return;
+        auto& c = counters[name];
+        c.first += v;
+        c.second += 1;
+    }
     std::vector<pma_ctx*> lanes;  // child contexts of batch calls (own stream and scratch)
     pma_limits limits{1 << 20, 1 << 22, (1ull << 23) - 1, 0};  // device loop bounds
-    bool reference_throat_ids = true;  // pma_pores numbers shared types as the reference does
+    bool reference_throat_ids = false;  // pma_pores numbers shared types as the reference does
     // Demand: the largest size each named buffer was asked for since reset_demand(), summed;
     // what one request needs, whatever earlier requests left in the cache.
     std::map<std::string, size_t> demand;

@@ -69,6 +69,7 @@ struct WsState {
     unsigned int* pbound;         // per pore
     unsigned int* err;
     int spin_limit;               // polls of one wait on another block before giving up
+    unsigned long long* gen_hist; // NULL, or generations counted by log2 of their frontier size
     uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
     unsigned int* bfill;
@@ -337,6 +338,7 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
         const unsigned long long nev = static_cast<unsigned long long>(__ldcg(ng + cur)) * 27;
         if (nev == 0) break;
         ++gen;
+        if (s.gen_hist && tid == 0) atomicAdd(&s.gen_hist[min(63, 63 - __clzll(nev / 27))], 1ull);
         const uint32_t* gv = cur ? gv1 : gv0;
         const uint32_t* gp = cur ? gp1 : gp0;
         uint32_t* nv = cur ? gv0 : gv1;
@@ -677,6 +679,11 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ws.ext_count = reinterpret_cast<unsigned int*>(d_count + 1);
     ws.err = reinterpret_cast<unsigned int*>(d_count + 2);
     ws.spin_limit = ctx->limits.spin_limit;
+    ws.gen_hist = nullptr;
+    if (ctx->timing) {  // frontier sizes of the generations, for the timing report
+        ws.gen_hist = buf<unsigned long long>(ctx, "ws.gen_hist", 64);
+        PMA_CUDA(cudaMemsetAsync(ws.gen_hist, 0, 64 * 8, s));
+    }
     ws.pbound = buf<unsigned int>(ctx, "ws.pbound", npores);
     // Shared-voxel records: a first guess of n/32; the pool doubles (copying the records)
     // whenever it is more than half used at a host synchronisation point, and a flood that
@@ -843,6 +850,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
                 PMA_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ws_generations), coop_grid,
                                                      kChunk / 4, args, 0, s));
                 ctx->count_launch(1);
+                ctx->count("ws.cooperative_launches", 1);
                 {
                     ReadBack rb;
                     rb.add(h_out, d_out, 16);
@@ -871,6 +879,13 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     PMA_REQUIRE(!(h_err & 2u), PMA_ERR_INTERNAL, "pma_watershed: a shared voxel recorded more pores than touch it");
     PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
     PMA_REQUIRE(!(h_err & 16u), PMA_ERR_LIMIT, "pma_watershed: frontier compaction look-back did not finish");
+    if (ws.gen_hist) {
+        unsigned long long hh[64];
+        PMA_CUDA(cudaMemcpyAsync(hh, ws.gen_hist, sizeof(hh), cudaMemcpyDeviceToHost, s));
+        ctx->sync();
+        for (int b = 0; b < 64; ++b)
+            if (hh[b]) ctx->count("ws.generations.frontier_2^" + std::to_string(b), static_cast<double>(hh[b]));
+    }
 
     KernelTimer kt_tables(ctx, "ws_tables");  // to the end of the stage
     // Volumes, labels and shared voxels.

@@ -35,6 +35,7 @@ def ctx(pma_lib):
     import porousmediaanalysis_gb300 as pma
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"
     c = pma.Context(0)
+    c.set_throat_numbering(reference=True)  # parity: the reference's own shared-type ids
     yield c
     c.close()
 

@@ -115,3 +115,30 @@ def test_run_folder_reports_errors(ctx, tmp_path):
     with pytest.raises(pma.PmaError) as e:
         pma.run_folder(ctx, str(tmp_path), pma.MODE_ALL)
     assert "Images" in str(e.value)
+
+
+@pytest.mark.parametrize("name,case,resolution", [("pack_odd_z2", "pack_odd", "1 1 2"),
+                                                  ("pack_odd_xy", "pack_odd", "2 1.5 1"),
+                                                  ("union_small_xyz", "union_small", "1.5 2 1.25")])
+def test_run_folder_resamples_the_input_stack(ctx, tmp_path, texts, name, case, resolution):
+    """A resolution other than 1 1 1 makes -all and -spd resample Images/ first
+    (ImageResampler.cpp:28-67): Original/ keeps the slices, Images/ gets the repeated and
+    in-plane upsampled ones, and every later stage runs on those. Compared with the reference
+    run (with FreeImage's own resize engine) on the same folder."""
+    import porousmediaanalysis_gb300 as pma
+    from porousmediaanalysis_gb300 import capi
+    vol, d3q7 = make_case(case)
+    sample = make_sample(str(tmp_path), vol, d3q7, resolution)
+    pma.run_folder(ctx, str(tmp_path), pma.MODE_ALL)
+    pma.run_folder(ctx, str(tmp_path), pma.MODE_SPD)  # Original/ exists: no second resampling
+    ref = texts[name]
+    images = capi.read_tiff_stack(os.path.join(sample, "Images"), 1)
+    assert list(images.shape) == ref["shape"]
+    assert digest(images) == ref["digests"]["Images"]
+    assert np.array_equal(capi.read_tiff_stack(os.path.join(sample, "Original"), 1),
+                          np.where(vol != 0, 255, 0).astype(np.uint8))
+    for fname in EXACT_TEXTS:
+        with open(os.path.join(sample, fname)) as f:
+            assert f.read() == ref[fname], fname
+    for fname, bpv in FOLDERS.items():
+        assert digest(capi.read_tiff_stack(os.path.join(sample, fname), bpv)) == ref["digests"][fname], fname
