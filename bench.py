@@ -38,6 +38,8 @@ WORKLOADS = {
                          desc="1024^3 leveled-wave spinodal, 1000 waves, wavelength 48, porosity 0.70"),
     "spinodal384": dict(kind="spinodal", shape=(384, 384, 384), seed=3,
                         desc="384^3 leveled-wave spinodal, 1000 waves, wavelength 48, porosity 0.70 (profiling size)"),
+    "spinodal256": dict(kind="spinodal", shape=(256, 256, 256), seed=3,
+                        desc="256^3 leveled-wave spinodal, 1000 waves, wavelength 48, porosity 0.70 (profiling size)"),
     "union128": dict(kind="union", shape=(128, 128, 128), seed=1,
                      desc="128^3 union of 300 spheres, radii U[5,10]"),
 }

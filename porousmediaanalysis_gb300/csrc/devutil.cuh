@@ -8,18 +8,44 @@
 
 namespace pma {
 
+// Division of 32-bit values by a divisor fixed in advance, as a multiply-high, an add and a
+// shift (the "round-up" magic-number method of Granlund and Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(m, n) + n) >> l for every n < 2^32.
+struct FastDiv {
+    uint32_t d = 1, m = 1, l = 0;
+    FastDiv() = default;
+    __host__ __device__ explicit FastDiv(uint32_t divisor) : d(divisor) {
+        l = 0;
+        while (l < 32 && (1ull << l) < divisor) ++l;
+        m = static_cast<uint32_t>(((1ull << 32) * ((1ull << l) - divisor)) / divisor + 1);
+    }
+    __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+        const uint32_t t = __umulhi(m, n);
+#else
+        const uint32_t t = static_cast<uint32_t>((static_cast<unsigned long long>(m) * n) >> 32);
+#endif
+        return static_cast<uint32_t>((static_cast<unsigned long long>(t) + n) >> l);
+    }
+};
+
 struct Grid {
     int SX, SY, SZ;
+    FastDiv fy, fx;  // division by SY and by SX
+    Grid() = default;
+    __host__ __device__ Grid(int sx, int sy, int sz)
+        : SX(sx), SY(sy), SZ(sz), fy(static_cast<uint32_t>(sy)), fx(static_cast<uint32_t>(sx)) {}
     __host__ __device__ __forceinline__ size_t idx(int x, int y, int z) const {
         return (static_cast<size_t>(z) * SX + x) * SY + y;
     }
-    // Volumes hold fewer than 2^32 voxels, so the division runs in 32 bits (a 64-bit
-    // integer division is several times longer and dominated the index-heavy kernels).
+    // Volumes hold fewer than 2^32 voxels, so the divisions run in 32 bits, by multiplication
+    // (the index-heavy kernels spend most of their instructions here otherwise).
     __host__ __device__ __forceinline__ void coords(size_t v, int& x, int& y, int& z) const {
         const uint32_t v32 = static_cast<uint32_t>(v);
-        const uint32_t zx = v32 / static_cast<uint32_t>(SY);
+        const uint32_t zx = fy.div(v32);
         y = static_cast<int>(v32 - zx * static_cast<uint32_t>(SY));
-        const uint32_t zz = zx / static_cast<uint32_t>(SX);
+        const uint32_t zz = fx.div(zx);
         x = static_cast<int>(zx - zz * static_cast<uint32_t>(SX));
         z = static_cast<int>(zz);
     }
