@@ -44,6 +44,9 @@ template <> struct Bits<double> {
 
 struct Geo {
     int SX, SY, SZ;
+    FastDiv fy, fx;  // division by SY and by SX (multiply-high)
+    Geo() = default;
+    Geo(int sx, int sy, int sz) : SX(sx), SY(sy), SZ(sz), fy(static_cast<uint32_t>(sy)), fx(static_cast<uint32_t>(sx)) {}
     __device__ __forceinline__ size_t idx(int x, int y, int z) const {
         return (static_cast<size_t>(z) * SX + x) * SY + y;
     }
@@ -146,10 +149,11 @@ __global__ void __launch_bounds__(256) geo_bucket(Geo g, T w1, T w2, T w3, T* __
         const uint32_t v = list[i];
         const T dv = dist[v];
         if (Bits<T>::bucket(dv) != k) continue;  // stale: the voxel moved to a lower bucket
-        const int y = static_cast<int>(v % g.SY);
-        const uint32_t zx = v / g.SY;
-        const int x = static_cast<int>(zx % g.SX);
-        const int z = static_cast<int>(zx / g.SX);
+        const uint32_t zx = g.fy.div(v);
+        const int y = static_cast<int>(v - zx * static_cast<uint32_t>(g.SY));
+        const uint32_t zz = g.fx.div(zx);
+        const int x = static_cast<int>(zx - zz * static_cast<uint32_t>(g.SX));
+        const int z = static_cast<int>(zz);
         cavity[v] = cavity_id;
         ++my_settled;
         const bool xl = x > 0, xh = x < g.SX - 1, yl = y > 0, yh = y < g.SY - 1, zl = z > 0, zh = z < g.SZ - 1;

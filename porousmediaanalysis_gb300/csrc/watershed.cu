@@ -70,6 +70,7 @@ struct WsState {
     unsigned int* err;
     int spin_limit;               // polls of one wait on another block before giving up
     unsigned long long* gen_hist; // NULL, or generations counted by log2 of their frontier size
+    int time_shift;               // bucket entry time = (generation << time_shift) | event
     uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
     unsigned int* bfill;
@@ -246,7 +247,7 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
         }
         const unsigned pos = atomicAdd(&s.bfill[r], 1u);
         const unsigned long long at = s.boff[r] + pos;
-        s.ent_time[at] = (gen << 40) | seq;
+        s.ent_time[at] = (gen << s.time_shift) | seq;
         s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
         return false;
     }
@@ -756,6 +757,10 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         auto* srt_time = buf<unsigned long long>(ctx, "ws.srt_time", max_bucket);
         auto* srt_val = buf<unsigned long long>(ctx, "ws.srt_val", max_bucket);
         const size_t max_events = max_bucket * 27;
+        // bucket entry times: events (and the seeds' pore indices) below 2^time_shift, so that a
+        // depth's sort needs only time_shift + bits(generation) key bits
+        ws.time_shift = 1;
+        while (ws.time_shift < 41 && (1ull << ws.time_shift) <= std::max<size_t>(max_events, npores)) ++ws.time_shift;
 
         ws.ev_touch = buf<uint8_t>(ctx, "ws.ev_touch", max_events);  // written for every event by phase 0
         // chunk descriptors of the frontier compaction; generations restart at 1 in this attempt
@@ -831,8 +836,10 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
                                                  static_cast<unsigned>(n0), gvb[cur], gpb[cur], d_ng + cur);
                 ctx->check_launch("ws_sort_small");
             } else {
+                int gen_bits = 0;
+                while (gen_bits < 24 && (1ull << gen_bits) <= gen) ++gen_bits;
                 sort_pairs(ctx, ws.ent_time + boff[depth], srt_time, ws.ent_val + boff[depth], srt_val,
-                           static_cast<int64_t>(n0));
+                           static_cast<int64_t>(n0), std::min(64, ws.time_shift + gen_bits));
                 ws_unpack_entries<<<grid_for(ctx, n0), 256, 0, s>>>(srt_val, n0, gvb[cur], gpb[cur]);
                 ctx->check_launch("ws_unpack_entries");
                 h_small[2] = static_cast<unsigned int>(n0);
