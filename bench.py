@@ -218,28 +218,25 @@ def run_batch(pma, ctx, dev, lanes, reps):
 SERVE_SIDES = (64, 128, 256, 384, 512, 768)
 
 
-def run_serving(args):
-    """Serving: Poisson arrivals of cubic requests (side uniform in SERVE_SIDES, structure
+def run_serving(args, pma, ctx, requests, sides=SERVE_SIDES, variants=2):
+    """Serving: Poisson arrivals of cubic requests (side uniform in `sides`, structure
     alternating between a Gaussian random field with sigma U[2,6], porosity U[0.5,0.8] and a
-    sphere pack with radii U[3,12], solid 0.40) at ~80% of the plain form's throughput, under
-    a 160 GB device-memory budget. Prints one JSON line with p50/p99 latency and throughput."""
+    sphere pack with radii U[3,12], solid 0.40) at args.serve_load of the plain form's
+    throughput, admitted under args.serve_budget_gb of device memory. `variants` distinct
+    volumes per (side, structure) are generated up front and drawn at random. Returns the JSON
+    object with p50/p99 latency and throughput."""
     import numpy as np
     import torch
-    import porousmediaanalysis_gb300 as pma
-    from porousmediaanalysis_gb300 import build as pbuild, synth
-    pbuild.build()
-    torch.cuda.set_device(0)
-    ctx = pma.Context(0)
+    from porousmediaanalysis_gb300 import synth
     rng = np.random.default_rng(5)
     reqs = []
-    for i in range(args.serve_requests):
-        side = int(rng.choice(SERVE_SIDES))
-        reqs.append((side, "grf" if i % 2 == 0 else "pack", int(rng.integers(0, 2))))
-    # templates: two structures per (side, kind), reused across requests
+    for i in range(requests):
+        side = int(rng.choice(sides))
+        reqs.append((side, "grf" if i % 2 == 0 else "pack", int(rng.integers(0, variants))))
     templates = {}
     for key in sorted(set(reqs)):
         side, kind, var = key
-        trng = np.random.default_rng(side * 10 + (2 if kind == "grf" else 0) + var)
+        trng = np.random.default_rng(side * 1000 + (500 if kind == "grf" else 0) + var)
         if kind == "grf":
             v = synth.grf((side,) * 3, sigma=float(trng.uniform(2, 6)), porosity=float(trng.uniform(0.5, 0.8)),
                           seed=int(trng.integers(1 << 30)), device="cuda")
@@ -249,10 +246,10 @@ def run_serving(args):
         del v
     torch.cuda.empty_cache()
     fields = ("watershed_labels",)
-    # plain form: each template alone, one after another
+    # plain form: each distinct volume alone, one after another (a warm-up run first)
     alone = {}
     for key, vol in templates.items():
-        pma.pipeline_host(ctx, vol, fp64=True, fields=fields)  # warm-up
+        pma.pipeline_host(ctx, vol, fp64=True, fields=fields)
         t0 = time.perf_counter()
         pma.pipeline_host(ctx, vol, fp64=True, fields=fields)
         alone[key] = time.perf_counter() - t0
@@ -288,21 +285,33 @@ def run_serving(args):
     th.join()
     st = srv.stats()
     srv.close()
+    ctx.trim()
     lat_sorted = sorted(lat)
     pct = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(math.ceil(q * len(lat_sorted))) - 1)]
-    line = {
+    return {
         "metric": "serving", "value": total_vox / (t_end - t_start) / 1e9, "unit": "Gvoxel/s",
-        "n_gpus": 1, "higher_is_better": True, "data": "synthetic", "dtype": "u32+f64",
         "p50_ms": pct(0.50), "p99_ms": pct(0.99), "mean_ms": sum(lat) / len(lat),
         "plain_value": plain_tput / 1e9, "offered_load": args.serve_load, "requests": len(reqs),
-        "arrival_rate_per_s": rate, "lanes": args.serve_lanes, "memory_budget_bytes": budget,
-        "max_in_flight": st["max_in_flight"], "peak_reserved_bytes": st["peak_reserved_bytes"],
-        "bytes_per_voxel": st["bytes_per_voxel"],
-        "rejected": st["rejected"], "failed": st["failed"],
-        "config": {"workload": "serving", "sides": SERVE_SIDES, "templates": len(templates),
-                   "outputs": "watershed labels to host; geodesics float64 kept on device",
-                   "desc": "Poisson arrivals at %.0f%% of the plain form's throughput" % (100 * args.serve_load)},
-    }
+        "distinct_volumes": len(templates), "arrival_rate_per_s": rate, "lanes": args.serve_lanes,
+        "memory_budget_bytes": budget, "max_in_flight": st["max_in_flight"],
+        "peak_reserved_bytes": st["peak_reserved_bytes"], "bytes_per_voxel": st["bytes_per_voxel"],
+        "rejected": st["rejected"], "failed": st["failed"], "sides": list(sides),
+        "desc": "Poisson arrivals at %.0f%% of the plain form's throughput; outputs: watershed labels to "
+                "host, float64 geodesics kept on the device" % (100 * args.serve_load)}
+
+
+def serve_main(args):
+    """The configured serving benchmark as its own JSON line."""
+    import torch
+    import porousmediaanalysis_gb300 as pma
+    from porousmediaanalysis_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    ctx = pma.Context(0)
+    res = run_serving(args, pma, ctx, args.serve_requests, variants=args.serve_variants)
+    line = dict(res)
+    line.update({"n_gpus": 1, "higher_is_better": True, "data": "synthetic", "dtype": "u32+f64",
+                 "config": {"workload": "serving", "sides": list(SERVE_SIDES)}})
     print(json.dumps(line))
     ctx.close()
 
@@ -402,13 +411,16 @@ def main():
                     help="lanes of the batched-form measurement (0: leave it out)")
     ap.add_argument("--batch-repeats", type=int, default=2)
     ap.add_argument("--serve", action="store_true", help="run the serving benchmark instead")
-    ap.add_argument("--serve-requests", type=int, default=120)
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-variants", type=int, default=8, help="distinct volumes per (side, structure)")
     ap.add_argument("--serve-lanes", type=int, default=8)
-    ap.add_argument("--serve-budget-gb", type=float, default=160.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--serve-load", type=float, default=0.8)
+    ap.add_argument("--serve-short", type=int, default=48,
+                    help="requests of the short serving run in the default line (0: leave it out)")
     args = ap.parse_args()
     if args.serve:
-        return run_serving(args)
+        return serve_main(args)
     if args.impl == "reference":
         return run_reference(args, args.workload)
 
@@ -528,6 +540,14 @@ def main():
     if args.batch_lanes > 0:
         batch = run_batch(pma, ctx, dev, args.batch_lanes, args.batch_repeats)
 
+    serving = None
+    if args.serve_short > 0 and rank == 0:
+        del solid
+        torch.cuda.empty_cache()
+        ctx.trim()
+        # a short run of the serving loop (the configured 2000-request run: bench.py --serve)
+        serving = run_serving(args, pma, ctx, args.serve_short, sides=(64, 128, 256, 384), variants=2)
+
     if rank == 0:
         line = {
             "metric": "pipeline_throughput", "value": value, "unit": "Gvoxel/s", "n_gpus": world,
@@ -545,6 +565,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "batch": batch,
+            "serving": serving,
         }
         print(json.dumps(line))
     ctx.close()

@@ -21,6 +21,14 @@
 // Frontier sizes stay on the device; the next generation is compacted in event order (see
 // ws_generations).
 //
+// Voxel state: one 64-bit word per voxel holds the claim state, which is the untouched mark,
+// the smallest touch of the running generation (kTouched | event), or the claimer (pore
+// index + 1). Claimed < touched < untouched numerically, so the claim phase's atomicMin keeps
+// the smallest touch and never undoes a claim; a touched voxel is always claimed by the
+// generation's resolve phase, so no touch outlives its generation. When the containing radii
+// fit 16 bits (radius below 256 voxels) they ride in the word's low bits: a touch then costs one
+// random load, and its atomic hits the same sector.
+//
 // Shared types: a voxel's key is its claimer plus its extending pores in time order; every
 // prefix of length >= 2 was created at the time of its last extension. All prefixes are
 // hashed, grouped with radix sorts and ranked by creation time on the device, which
@@ -43,7 +51,6 @@ namespace pma {
 namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
-constexpr unsigned long long kNoTime = ~0ull;
 constexpr int kSlots = 6;         // extending pores per record; a voxel chains more records
 constexpr int kMaxExt = 26;       // extending pores of one voxel at most (26 neighbours touch it)
 constexpr int kMaxHops = (kMaxExt + kSlots - 1) / kSlots;  // records in one voxel's chain
@@ -52,14 +59,16 @@ constexpr int kChunk = 1024;      // event slots per compaction block
 constexpr int kGensPerLaunch = 64;  // generations per cooperative launch (host checks between)
 constexpr unsigned long long kMaxGen = 1ull << 23;              // generations per call
 constexpr unsigned long long kSeqMask = (1ull << 40) - 1;       // touch time within a generation
+constexpr unsigned long long kUntouched = (1ull << 48) - 1;     // claim states (48-bit field)
+constexpr unsigned long long kTouched = 1ull << 46;
 constexpr uint32_t kRecBusy = 0xFFFFFFFFu;  // ext[w] while its record is being allocated
 
 struct WsState {
     Grid g;
     int d3q7;
     const uint32_t* crad;
-    uint32_t* claim;              // pore index + 1, 0 = unclaimed
-    unsigned long long* ckey;     // tagged claim time of the latest generation that touched it
+    unsigned long long* state;    // per voxel: claim state, << 16 | radius when packed
+    int packed;                   // 1: radii below 2^16 are held in the state words
     uint32_t* ext;                // shared-voxel record + 1, 0 = none
     uint32_t* ext_pore;           // [records][kSlots]
     unsigned long long* ext_time;
@@ -78,17 +87,42 @@ struct WsState {
     unsigned long long* ent_val;
 };
 
-__global__ void ws_init(size_t n, uint32_t* __restrict__ claim, unsigned long long* __restrict__ ckey,
-                        uint32_t* __restrict__ ext) {
+__host__ __device__ __forceinline__ unsigned long long ws_word(int packed, unsigned long long st, uint32_t r) {
+    return packed ? (st << 16) | r : st;
+}
+
+// Claim state of a state word: the claimer (pore index + 1) or 0.
+__device__ __forceinline__ uint32_t ws_claimer(int packed, unsigned long long word) {
+    const unsigned long long st = packed ? word >> 16 : word;
+    return st < kTouched ? static_cast<uint32_t>(st) : 0u;
+}
+
+// The radius and claim state of voxel w (one load when packed).
+__device__ __forceinline__ void ws_load(const WsState& s, size_t w, uint32_t& r, unsigned long long& st) {
+    const unsigned long long word = __ldcg(s.state + w);
+    if (s.packed) {
+        r = static_cast<uint32_t>(word & 0xFFFFu);
+        st = word >> 16;
+    } else {
+        r = __ldg(s.crad + w);
+        st = word;
+    }
+}
+
+__global__ void ws_init(size_t n, const uint32_t* __restrict__ crad, int packed,
+                        unsigned long long* __restrict__ state, uint32_t* __restrict__ ext) {
     PMA_GRID_STRIDE(v, n) {
-        claim[v] = 0;
-        ckey[v] = kNoTime;
+        state[v] = ws_word(packed, kUntouched, packed ? crad[v] : 0u);
         ext[v] = 0;
     }
 }
 
-__global__ void ws_seed(const uint32_t* __restrict__ seed_voxel, size_t np, uint32_t* __restrict__ claim) {
-    PMA_GRID_STRIDE(k, np) claim[seed_voxel[k]] = static_cast<uint32_t>(k + 1);
+__global__ void ws_seed(const uint32_t* __restrict__ seed_voxel, size_t np, const uint32_t* __restrict__ crad,
+                        int packed, unsigned long long* __restrict__ state) {
+    PMA_GRID_STRIDE(k, np) {
+        const uint32_t v = seed_voxel[k];
+        state[v] = ws_word(packed, k + 1, packed ? crad[v] : 0u);
+    }
 }
 
 __global__ void ws_seed_entries(const unsigned long long* __restrict__ a, size_t np,
@@ -174,10 +208,8 @@ __device__ __noinline__ void ws_extend(const WsState& s, size_t w, uint32_t pore
 }
 
 // Touch events of the generation's nodes. Phase 0 claims: the smallest touch time of each
-// unclaimed voxel wins. Claim keys carry a generation tag that decreases from one generation
-// to the next, so a key left by an earlier generation is larger than any key of the current
-// one and ckey never needs clearing. A touch of a voxel claimed in an earlier generation is
-// final in phase 0 already: it is an extension when the toucher is not the owner (claims
+// unclaimed voxel wins (atomicMin on its state word). A touch of a voxel claimed in an
+// earlier generation is final in phase 0 already: it is an extension when the toucher is not the owner (claims
 // never change, and extensions keep each pore's smallest time, so the order of recording
 // does not matter). Phase 0 flags, per event, a touch of an unclaimed voxel; phase 1 resolves
 // only those: the winner records its claim, and every other touch by a pore other than the
@@ -187,8 +219,7 @@ __device__ __noinline__ void ws_extend(const WsState& s, size_t w, uint32_t pore
 // other blocks earlier in the launch is read with __ldcg (L2, not a possibly stale L1 line);
 // only the radii, which never change, go through the read-only path.
 __device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t* gv, const uint32_t* gp,
-                                               unsigned long long seq, uint32_t depth, unsigned long long gen,
-                                               unsigned long long tag) {
+                                               unsigned long long seq, uint32_t depth, unsigned long long gen) {
     const unsigned long long i = seq / 27;
     const int j = static_cast<int>(seq - i * 27);
     uint8_t touched = 0;
@@ -203,14 +234,14 @@ __device__ __forceinline__ void ws_claim_event(const WsState& s, const uint32_t*
             s.pbound[pore] = 1;
         } else {
             const size_t w = s.g.idx(nx, ny, nz);
-            // both loads in flight at once; the claim is only used for a touched voxel
-            const uint32_t r = __ldg(s.crad + w);
-            const uint32_t c = __ldcg(s.claim + w);
+            uint32_t r;
+            unsigned long long st;
+            ws_load(s, w, r, st);
             if (r != 0 && r <= depth) {  // WC.cpp:152-156
-                if (c == 0) {
-                    atomicMin(&s.ckey[w], (tag << 40) | seq);
+                if (st >= kTouched) {
+                    atomicMin(&s.state[w], ws_word(s.packed, kTouched | seq, r));
                     touched = 1;
-                } else if (c - 1 != pore) {
+                } else if (st - 1 != pore) {
                     ws_extend(s, w, pore, (gen << 40) | seq);
                 }
             }
@@ -236,10 +267,11 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
     // the neighbour is inside the box (phase 0 touched it)
     const size_t w = static_cast<size_t>(static_cast<long long>(v) +
                                          (static_cast<long long>(dz) * s.g.SX + dx) * s.g.SY + dy);
-    const unsigned long long wseq = __ldcg(s.ckey + w) & kSeqMask;
-    if (wseq == seq) {
-        s.claim[w] = pore + 1;
-        const uint32_t r = __ldg(s.crad + w);
+    uint32_t r;
+    unsigned long long st;
+    ws_load(s, w, r, st);
+    if (st == (kTouched | seq)) {
+        s.state[w] = ws_word(s.packed, pore + 1, r);  // one 64-bit store: readers see either word
         if (r == depth) {
             nw = static_cast<uint32_t>(w);
             np_out = pore;
@@ -251,7 +283,8 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
         s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
         return false;
     }
-    const uint32_t owner = __ldcg(gp + wseq / 27);
+    // the winner's pore: already stored as the claimer, or that of the winning touch's node
+    const uint32_t owner = st < kTouched ? static_cast<uint32_t>(st - 1) : __ldcg(gp + (st & kSeqMask) / 27);
     if (owner != pore) ws_extend(s, w, pore, (gen << 40) | seq);
     return false;
 }
@@ -344,8 +377,7 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
         const uint32_t* gp = cur ? gp1 : gp0;
         uint32_t* nv = cur ? gv0 : gv1;
         uint32_t* np_ = cur ? gp0 : gp1;
-        const unsigned long long tag = kMaxGen - gen;
-        for (unsigned long long seq = tid; seq < nev; seq += stride) ws_claim_event(s, gv, gp, seq, depth, gen, tag);
+        for (unsigned long long seq = tid; seq < nev; seq += stride) ws_claim_event(s, gv, gp, seq, depth, gen);
         grid.sync();
         // Resolve by chunks of kChunk events: event k * blockDim + t of a chunk is thread t's
         // k-th, so event order is k-major, then thread.
@@ -446,12 +478,13 @@ __global__ void ws_unpack_entries(const unsigned long long* __restrict__ val, si
     }
 }
 
-__global__ void ws_volumes(const uint32_t* __restrict__ claim, const uint32_t* __restrict__ ext, size_t n,
-                           unsigned long long* __restrict__ pvol, uint8_t* __restrict__ shared_flag) {
+__global__ void ws_volumes(const unsigned long long* __restrict__ state, int packed,
+                           const uint32_t* __restrict__ ext, size_t n, unsigned long long* __restrict__ pvol,
+                           uint8_t* __restrict__ shared_flag) {
     // lanes of a warp claimed by the same pore combine their counts
     const unsigned lane = threadIdx.x & 31;
     PMA_GRID_STRIDE(v, n) {
-        const uint32_t c = claim[v];
+        const uint32_t c = ws_claimer(packed, state[v]);
         const bool sh = ext[v] != 0;
         shared_flag[v] = sh;
         const uint32_t key = (c && !sh) ? c : 0u;
@@ -501,7 +534,8 @@ __global__ void ws_key_lengths(const uint32_t* __restrict__ sv, size_t ns, const
 // Key of shared voxel i: [first extension, claimer, later extensions...] in pore indices, at
 // kseq[koff[i] ..], and one record per prefix of length L = 2..len at record
 // koff[i] - i + L - 2 (its hashes, creation time and voxel).
-__global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const uint32_t* __restrict__ claim,
+__global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const unsigned long long* __restrict__ state,
+                        int packed,
                         const uint32_t* __restrict__ ext, const uint32_t* __restrict__ ext_pore,
                         const unsigned long long* __restrict__ ext_time, const uint32_t* __restrict__ ext_next,
                         const unsigned long long* __restrict__ koff, uint32_t* __restrict__ kseq,
@@ -523,7 +557,7 @@ __global__ void ws_keys(const uint32_t* __restrict__ sv, size_t ns, const uint32
             }
         uint32_t key[kKeyMax];
         key[0] = p[0];
-        key[1] = claim[v] - 1;
+        key[1] = ws_claimer(packed, state[v]) - 1;
         for (int k = 1; k < m; ++k) key[k + 1] = p[k];
         const int len = m + 1;
         const unsigned long long base = koff[i];
@@ -607,10 +641,10 @@ __global__ void ws_group_reduce(const uint32_t* __restrict__ rec, const uint32_t
     }
 }
 
-__global__ void ws_labels(const uint32_t* __restrict__ claim, size_t n, const uint32_t* __restrict__ pore_id,
-                          uint32_t* __restrict__ labels) {
+__global__ void ws_labels(const unsigned long long* __restrict__ state, int packed, size_t n,
+                          const uint32_t* __restrict__ pore_id, uint32_t* __restrict__ labels) {
     PMA_GRID_STRIDE(v, n) {
-        const uint32_t c = claim[v];
+        const uint32_t c = ws_claimer(packed, state[v]);
         labels[v] = c ? pore_id[c - 1] : 0u;
     }
 }
@@ -674,8 +708,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ws.g = g;
     ws.d3q7 = st == PMA_D3Q7 ? 1 : 0;
     ws.crad = crad2;
-    ws.claim = buf<uint32_t>(ctx, "ws.claim", n);
-    ws.ckey = buf<unsigned long long>(ctx, "ws.ckey", n);
+    ws.state = buf<unsigned long long>(ctx, "ws.state", n);
+    ws.packed = max_edt2 < 65536u ? 1 : 0;  // radii up to max_edt2 fit the word's low 16 bits
     ws.ext = buf<uint32_t>(ctx, "ws.ext", n);
     ws.ext_count = reinterpret_cast<unsigned int*>(d_count + 1);
     ws.err = reinterpret_cast<unsigned int*>(d_count + 2);
@@ -730,7 +764,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         PMA_CUDA(cudaMemsetAsync(ws.ext_pore, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 4, s));
         PMA_CUDA(cudaMemsetAsync(ws.ext_time, 0xFF, static_cast<size_t>(ws.ext_cap) * kSlots * 8, s));
         PMA_CUDA(cudaMemsetAsync(ws.pbound, 0, std::max<size_t>(npores, 1) * 4, s));
-        ws_init<<<G, 256, 0, s>>>(n, ws.claim, ws.ckey, ws.ext);
+        ws_init<<<G, 256, 0, s>>>(n, crad2, ws.packed, ws.state, ws.ext);
         ctx->check_launch("ws_init");
 
         // Buckets: capacity = voxels of that crad + seeds of that radius.
@@ -783,7 +817,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
             ctx->check_launch("ws_seed_entries");
             uint32_t* d_seed = buf<uint32_t>(ctx, "ws.seedvox", npores);
             PMA_CUDA(cudaMemcpyAsync(d_seed, seed_voxel.data(), npores * 4, cudaMemcpyHostToDevice, s));
-            ws_seed<<<grid_for(ctx, npores), 256, 0, s>>>(d_seed, npores, ws.claim);
+            ws_seed<<<grid_for(ctx, npores), 256, 0, s>>>(d_seed, npores, crad2, ws.packed, ws.state);
             ctx->check_launch("ws_seed");
             ctx->sync();
         }
@@ -805,7 +839,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
         const unsigned coop_grid = static_cast<unsigned>(
             std::max<size_t>(1, std::min<size_t>(coop_need, static_cast<size_t>(ctx->num_sms) * std::min(per_sm, 8))));
         unsigned long long gen = 0;
-        // generations of this call at most: the context's bound, below the claim-key tag range
+        // generations of this call at most: the context's bound, within the entry-time range
         const unsigned long long max_gen =
             std::min<unsigned long long>(ctx->limits.watershed_generations, kMaxGen - 1);
         unsigned int* h_small = static_cast<unsigned int*>(ctx->host_staging(64));
@@ -899,13 +933,13 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     auto* pvol = buf<unsigned long long>(ctx, "ws.pvol", npores);
     uint8_t* shared_flag = buf<uint8_t>(ctx, "ws.shared_flag", n);
     PMA_CUDA(cudaMemsetAsync(pvol, 0, std::max<size_t>(npores, 1) * 8, s));
-    ws_volumes<<<G, 256, 0, s>>>(ws.claim, ws.ext, n, pvol, shared_flag);
+    ws_volumes<<<G, 256, 0, s>>>(ws.state, ws.packed, ws.ext, n, pvol, shared_flag);
     ctx->check_launch("ws_volumes");
     std::vector<uint32_t> pore_id(std::max<size_t>(npores, 1));
     for (size_t k = 0; k < npores; ++k) pore_id[k] = pores[k].id;
     uint32_t* d_pid = buf<uint32_t>(ctx, "ws.pid", pore_id.size());
     PMA_CUDA(cudaMemcpyAsync(d_pid, pore_id.data(), pore_id.size() * 4, cudaMemcpyHostToDevice, s));
-    ws_labels<<<G, 256, 0, s>>>(ws.claim, n, d_pid, labels);
+    ws_labels<<<G, 256, 0, s>>>(ws.state, ws.packed, n, d_pid, labels);
     ctx->check_launch("ws_labels");
     uint32_t* sv = buf<uint32_t>(ctx, "ws.sv", n);
     const int64_t nsh = select_flagged(ctx, thrust::counting_iterator<uint32_t>(0), shared_flag, sv,
@@ -948,7 +982,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     auto* rh2 = buf<unsigned long long>(ctx, "ws.rh2", nr);
     auto* rtime = buf<unsigned long long>(ctx, "ws.rtime", nr);
     uint32_t* rvox = buf<uint32_t>(ctx, "ws.rvox", nr);
-    ws_keys<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.claim, ws.ext, ws.ext_pore, ws.ext_time, ws.ext_next,
+    ws_keys<<<grid_for(ctx, nsh), 256, 0, s>>>(sv, nsh, ws.state, ws.packed, ws.ext, ws.ext_pore, ws.ext_time, ws.ext_next,
                                                koff, kseq, rh1, rh2, rtime, rvox);
     ctx->check_launch("ws_keys");
     uint32_t* rec = buf<uint32_t>(ctx, "ws.rec", nr);

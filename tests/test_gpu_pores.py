@@ -201,3 +201,21 @@ def test_cheaper_type_numbering_is_a_renaming(ctx, oracle_mod):
     assert sorted((t[2], t[1]) for t in t0) == sorted((t[2], t[1]) for t in r.throats0)
     assert (canonical_throats(g["labels_initial"]) == canonical_throats(r.labels_initial)).all()
     assert (g["ws"] == r.labels_ws).all() and g["ws_table"] == (r.pores_ws, r.throats_ws)
+
+
+def test_watershed_with_radii_beyond_16_bits(ctx, oracle_mod):
+    """Containing radii squared of 65536 and more (a void box 900 voxels long in X, split by a
+    solid wall with one hole; no solids bound Y or Z) take the watershed's unpacked state path;
+    the two pores meet at the hole, and the result equals the oracle's."""
+    vol = np.zeros((4, 900, 5), np.uint8)
+    vol[:, 450, :] = 1
+    vol[2, 450, 2] = 0
+    vol[1, 200, 3] = 1
+    g = _gpu_pipeline(ctx, vol, False)
+    o = oracle_mod.full(vol, geodesic_too=False)
+    assert o["max_edt2"] >= 65536
+    r = o["pores"]
+    assert len(r.throats_ws) >= 2
+    assert g["table"] == (r.pores, r.throats)
+    assert (g["ws"] == r.labels_ws).all()
+    assert g["ws_table"] == (r.pores_ws, r.throats_ws)
