@@ -479,6 +479,18 @@ T* buf(pma_ctx* ctx, const char* tag, size_t count) {
     return static_cast<T*>(ctx->scratch(tag, std::max<size_t>(count, 1) * sizeof(T)));
 }
 
+// Tile counts as 64-bit values, with a zero past the end (the scan then gives the total).
+__global__ void widen_counts(const unsigned int* __restrict__ c, size_t n, unsigned long long* __restrict__ out) {
+    PMA_GRID_STRIDE(i, n + 1) out[i] = i < n ? c[i] : 0ull;
+}
+
+// Offsets of the first tile of each z-slab (and the total at tz).
+__global__ void slab_offsets(const unsigned long long* __restrict__ toff, size_t per_z, int tz,
+                             unsigned long long* __restrict__ zoff) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z <= tz) zoff[z] = toff[static_cast<size_t>(z) * per_z];
+}
+
 }  // namespace
 
 void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t max_edt2,
@@ -539,21 +551,28 @@ void containing_balls(pma_ctx* ctx, const uint32_t* edt2, pma_dims d, uint32_t m
         balls_tile_count<<<grid_for(ctx, nc), 256, 0, s>>>(edt2, cand, nc, g, t, floor, tcount);
         ctx->check_launch("balls_tile_count");
     }
-    std::vector<unsigned int> hc(ntiles);
-    PMA_CUDA(cudaMemcpyAsync(hc.data(), tcount, ntiles * 4, cudaMemcpyDeviceToHost, s));
+    // 64-bit list offsets by a device scan; the host reads back only the offsets at the tile
+    // z-slab boundaries, which choose the slabs that fit the memory budget
+    auto* tc64 = buf<unsigned long long>(ctx, "balls.tc64", ntiles + 1);
+    widen_counts<<<grid_for(ctx, ntiles + 1), 256, 0, s>>>(tcount, ntiles, tc64);
+    ctx->check_launch("widen_counts");
+    exclusive_sum(ctx, tc64, toff, static_cast<int64_t>(ntiles + 1));
+    auto* zoff = buf<unsigned long long>(ctx, "balls.zoff", t.TZ + 1);
+    slab_offsets<<<div_up(t.TZ + 1, 256), 256, 0, s>>>(toff, per_z, t.TZ, zoff);
+    ctx->check_launch("slab_offsets");
+    std::vector<unsigned long long> hz(t.TZ + 1);
+    PMA_CUDA(cudaMemcpyAsync(hz.data(), zoff, (t.TZ + 1) * 8ull, cudaMemcpyDeviceToHost, s));
     ctx->sync();
-    std::vector<unsigned long long> ho(ntiles + 1, 0);
-    for (size_t i = 0; i < ntiles; ++i) ho[i + 1] = ho[i] + hc[i];
-    PMA_CUDA(cudaMemcpyAsync(toff, ho.data(), (ntiles + 1) * 8, cudaMemcpyHostToDevice, s));
+    auto ho_at = [&](int z) { return hz[z]; };  // offset of the first tile of slab z
     size_t free_b = 0, total_b = 0;
     PMA_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const unsigned long long budget = std::max<unsigned long long>(
         1ull << 20, std::min<unsigned long long>(free_b / 3, 32ull << 30) / 8);
     for (int z0 = 0; z0 < t.TZ;) {
         int z1 = z0 + 1;
-        while (z1 < t.TZ && ho[(z1 + 1) * per_z] - ho[z0 * per_z] <= budget) ++z1;
-        const unsigned long long base = ho[z0 * per_z];
-        const unsigned long long cnt = ho[z1 * per_z] - base;
+        while (z1 < t.TZ && ho_at(z1 + 1) - ho_at(z0) <= budget) ++z1;
+        const unsigned long long base = ho_at(z0);
+        const unsigned long long cnt = ho_at(z1) - base;
         auto* entries = buf<unsigned long long>(ctx, "balls.entries", cnt);
         if (nc) {
             KernelTimer kt(ctx, "balls_tile_fill");

@@ -55,8 +55,6 @@ struct Geo {
 struct Frontier {
     uint32_t* bits;        // four bitmaps of nwords words: bucket b uses bitmap b & 3
     size_t nwords;
-    uint32_t* summary;     // four summaries of nsum words: bit i = bitmap word i is non-zero
-    size_t nsum;
     unsigned int* count;   // [4] voxels set in each bitmap
     uint32_t* list;        // the compacted bucket being swept
     unsigned int* list_n;  // its length
@@ -77,41 +75,26 @@ __global__ void geo_init(const uint8_t* __restrict__ solid, size_t n, T* __restr
     }
 }
 
-// Sets voxel w in bitmap b; returns true when it was not set. A word that was empty gets
-// its summary bit, so that compaction visits only the words that hold voxels.
-__device__ __forceinline__ bool geo_push(const Frontier& f, int b, size_t w) {
-    const uint32_t bit = 1u << (w & 31);
-    const size_t word = w >> 5;
-    const uint32_t old = atomicOr(&f.bits[static_cast<size_t>(b) * f.nwords + word], bit);
-    if (old == 0) atomicOr(&f.summary[static_cast<size_t>(b) * f.nsum + (word >> 5)], 1u << (word & 31));
-    return !(old & bit);
-}
-
 template <class T>
 __global__ void geo_start(Frontier f, T* dist, uint32_t v) {
     dist[v] = static_cast<T>(0);
-    geo_push(f, 0, v);  // bucket 0
+    f.bits[v >> 5] |= 1u << (v & 31);  // bucket 0
     f.count[0] = 1;
 }
 
-// Bucket k's bitmap -> list, cleared behind. One warp per summary word: only the bitmap words
-// that hold voxels are read (a bucket is a thin shell of the volume); a warp's 32 words are
-// listed in voxel order.
+// Bucket k's bitmap -> list (voxel order within each block's 8192 voxels), cleared behind.
 __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
-    const unsigned lane = threadIdx.x & 31;
+    __shared__ unsigned int wsum[8];
+    __shared__ unsigned int base;
     uint32_t* bm = f.bits + static_cast<size_t>(k & 3) * f.nwords;
-    uint32_t* sm = f.summary + static_cast<size_t>(k & 3) * f.nsum;
-    const size_t nwarps = static_cast<size_t>(gridDim.x) * (blockDim.x >> 5);
-    for (size_t sw = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); sw < f.nsum;
-         sw += nwarps) {
-        const uint32_t sword = sm[sw];
-        if (!sword) continue;  // warp-uniform
-        if (lane == 0) sm[sw] = 0;
-        const size_t w = sw * 32 + lane;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (size_t w0 = static_cast<size_t>(blockIdx.x) * blockDim.x; w0 < f.nwords;
+         w0 += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t w = w0 + threadIdx.x;
         uint32_t word = 0;
-        if ((sword >> lane) & 1u) {
+        if (w < f.nwords) {
             word = bm[w];
-            bm[w] = 0;
+            if (word) bm[w] = 0;
         }
         const unsigned c = __popc(word);
         unsigned incl = c;
@@ -119,9 +102,19 @@ __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
             const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
             if (lane >= static_cast<unsigned>(o)) incl += t;
         }
-        unsigned base = 0;
-        if (lane == 31 && incl) base = atomicAdd(f.list_n, incl);
-        unsigned pos = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - c;
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int i = 0; i < 8; ++i) {
+                const unsigned v = wsum[i];
+                wsum[i] = tot;
+                tot += v;
+            }
+            base = tot ? atomicAdd(f.list_n, tot) : 0u;
+        }
+        __syncthreads();
+        unsigned pos = base + wsum[warp] + incl - c;
         while (word) {
             const int bit = __ffs(word) - 1;
             word &= word - 1;
@@ -129,6 +122,7 @@ __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
             else atomicExch(f.overflow, 1u);
             ++pos;
         }
+        __syncthreads();
     }
 }
 
@@ -149,6 +143,8 @@ __global__ void __launch_bounds__(256) geo_bucket(Geo g, T w1, T w2, T w3, T* __
     const long long sy = g.SY, sxy = static_cast<long long>(g.SX) * g.SY;
     unsigned long long my_settled = 0;
     unsigned my_walls = 0, c1 = 0, c2 = 0;
+    uint32_t* bm1 = f.bits + static_cast<size_t>((k + 1) & 3) * f.nwords;
+    uint32_t* bm2 = f.bits + static_cast<size_t>((k + 2) & 3) * f.nwords;
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t v = list[i];
         const T dv = dist[v];
@@ -191,10 +187,14 @@ __global__ void __launch_bounds__(256) geo_bucket(Geo g, T w1, T w2, T w3, T* __
                 const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
                 if (Bits<T>::to(nd) < old) {
                     const int pb = Bits<T>::bucket(nd);
-                    const bool fresh = geo_push(f, pb & 3, w);
-                    if (pb == k + 1) c1 += fresh ? 1u : 0u;
-                    else if (pb == k + 2) c2 += fresh ? 1u : 0u;
-                    else if (fresh) atomicAdd(&f.count[pb & 3], 1u);  // not reachable with steps in [1, 2)
+                    const uint32_t bit = 1u << (w & 31);
+                    if (pb == k + 1) {
+                        c1 += (atomicOr(&bm1[w >> 5], bit) & bit) ? 0u : 1u;
+                    } else if (pb == k + 2) {
+                        c2 += (atomicOr(&bm2[w >> 5], bit) & bit) ? 0u : 1u;
+                    } else if (!(atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit) & bit)) {
+                        atomicAdd(&f.count[pb & 3], 1u);  // not reachable with steps in [1, 2)
+                    }
                 }
             }
         }
@@ -274,16 +274,12 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
 
     const uint32_t cap = static_cast<uint32_t>(std::min<size_t>(n, size_t(1) << 28));
     const size_t nwords = (n + 31) / 32;
-    const size_t nsum = (nwords + 31) / 32;
     auto* bits = static_cast<uint32_t*>(ctx->scratch("geo.bits", 4 * nwords * 4));
-    auto* summary = static_cast<uint32_t*>(ctx->scratch("geo.summary", 4 * nsum * 4));
     auto* list = static_cast<uint32_t*>(ctx->scratch("geo.list", static_cast<size_t>(cap) * 4));
     auto* misc = static_cast<unsigned long long*>(ctx->scratch("geo.misc", 64));
     Frontier f;
     f.bits = bits;
     f.nwords = nwords;
-    f.summary = summary;
-    f.nsum = nsum;
     f.list = list;
     f.count = reinterpret_cast<unsigned int*>(misc);          // 4 x u32 = misc[0..1]
     f.overflow = reinterpret_cast<unsigned int*>(misc + 2);   // misc[2] low
@@ -293,7 +289,6 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
     f.list_n = reinterpret_cast<unsigned int*>(misc + 6);     // misc[6] low
     f.cap = cap;
     PMA_CUDA(cudaMemsetAsync(bits, 0, 4 * nwords * 4, s));
-    PMA_CUDA(cudaMemsetAsync(summary, 0, 4 * nsum * 4, s));
 
     geo_init<T><<<grid, 256, 0, s>>>(solid, n, dist, cavity);
     ctx->check_launch("geo_init");
@@ -314,7 +309,7 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
     const int max_buckets_per_sync = 32;
     const uint64_t bucket_limit = ctx->limits.geodesic_buckets ? ctx->limits.geodesic_buckets : 2ull * n + 64;
     const unsigned bucket_grid = static_cast<unsigned>(ctx->num_sms * 8);
-    const unsigned compact_grid = static_cast<unsigned>(std::min<size_t>(div_up(nsum, 8), ctx->num_sms * 8ull));
+    const unsigned compact_grid = static_cast<unsigned>(std::min<size_t>(div_up(nwords, 256), ctx->num_sms * 8ull));
     while (true) {  // SPC.cpp:94-140
         ++half;
         // SelectStartingPosition (SPC.cpp:396-426)

@@ -1306,6 +1306,12 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                 read_back(ctx, rb);
             }
             const unsigned long long nbig = h_info[1], total = h_info[2];
+            ctx->count("pores.levels", 1);
+            if (nbig) {
+                ctx->count("pores.big_sets", static_cast<double>(nbig));
+                ctx->count("pores.big_set_elements_expanded", static_cast<double>(total));
+            }
+            if (h_info[0]) ctx->count("pores.heavy_plateaus", static_cast<double>(h_info[0]));
             int64_t merged = 0;
             int shift = 32;
             void* keys = nullptr;
@@ -1382,6 +1388,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
                     }
                 }
             }
+            if (merged && !merged_dev) ctx->count("pores.big_set_elements_merged", static_cast<double>(merged));
             KernelTimer kt3(ctx, "level_write");
             exclusive_sum(ctx, ps.cnt, ps.off, static_cast<int64_t>(e - b));
             level_write<<<lg, kLevelWarps * 32, 0, s>>>(ps, b, e, base);

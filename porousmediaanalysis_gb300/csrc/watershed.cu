@@ -78,7 +78,8 @@ struct WsState {
     unsigned int* pbound;         // per pore
     unsigned int* err;
     int spin_limit;               // polls of one wait on another block before giving up
-    unsigned long long* gen_hist; // NULL, or generations counted by log2 of their frontier size
+    unsigned long long* gen_hist; // NULL, or per log2 of the frontier size: [c] generations,
+                                  // [64 + c] ns in claim phases, [128 + c] ns in resolve phases
     int time_shift;               // bucket entry time = (generation << time_shift) | event
     uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
@@ -352,6 +353,12 @@ __global__ void ws_wait_selftest(unsigned long long* desc, unsigned int* err, in
     ws_lookback(desc, 1, 1, 0, err, spin_limit, threadIdx.x & 31);
 }
 
+__device__ __forceinline__ unsigned long long ws_clock() {  // ns
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Up to max_gens generations of one depth in a single cooperative launch, two grid-wide
 // barriers per generation. ng[2] holds the two frontier sizes; the frontier starts on side
 // `cur`. out[0] = generations run, out[1] = the side holding the next frontier.
@@ -372,13 +379,23 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
         const unsigned long long nev = static_cast<unsigned long long>(__ldcg(ng + cur)) * 27;
         if (nev == 0) break;
         ++gen;
-        if (s.gen_hist && tid == 0) atomicAdd(&s.gen_hist[min(63, 63 - __clzll(nev / 27))], 1ull);
+        const int hc = min(63, 63 - __clzll(nev / 27));
+        unsigned long long t_start = 0;
+        if (s.gen_hist && tid == 0) {
+            atomicAdd(&s.gen_hist[hc], 1ull);
+            t_start = ws_clock();
+        }
         const uint32_t* gv = cur ? gv1 : gv0;
         const uint32_t* gp = cur ? gp1 : gp0;
         uint32_t* nv = cur ? gv0 : gv1;
         uint32_t* np_ = cur ? gp0 : gp1;
         for (unsigned long long seq = tid; seq < nev; seq += stride) ws_claim_event(s, gv, gp, seq, depth, gen);
         grid.sync();
+        if (s.gen_hist && tid == 0) {
+            const unsigned long long t = ws_clock();
+            atomicAdd(&s.gen_hist[64 + hc], t - t_start);
+            t_start = t;
+        }
         // Resolve by chunks of kChunk events: event k * blockDim + t of a chunk is thread t's
         // k-th, so event order is k-major, then thread.
         const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
@@ -421,6 +438,7 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
             __syncthreads();  // part is reused by the next chunk
         }
         grid.sync();
+        if (s.gen_hist && tid == 0) atomicAdd(&s.gen_hist[128 + hc], ws_clock() - t_start);
         cur ^= 1;
     }
     if (tid == 0) {
@@ -716,8 +734,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ws.spin_limit = ctx->limits.spin_limit;
     ws.gen_hist = nullptr;
     if (ctx->timing) {  // frontier sizes of the generations, for the timing report
-        ws.gen_hist = buf<unsigned long long>(ctx, "ws.gen_hist", 64);
-        PMA_CUDA(cudaMemsetAsync(ws.gen_hist, 0, 64 * 8, s));
+        ws.gen_hist = buf<unsigned long long>(ctx, "ws.gen_hist", 192);
+        PMA_CUDA(cudaMemsetAsync(ws.gen_hist, 0, 192 * 8, s));
     }
     ws.pbound = buf<unsigned int>(ctx, "ws.pbound", npores);
     // Shared-voxel records: a first guess of n/32; the pool doubles (copying the records)
@@ -921,11 +939,16 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
     PMA_REQUIRE(!(h_err & 16u), PMA_ERR_LIMIT, "pma_watershed: frontier compaction look-back did not finish");
     if (ws.gen_hist) {
-        unsigned long long hh[64];
+        unsigned long long hh[192];
         PMA_CUDA(cudaMemcpyAsync(hh, ws.gen_hist, sizeof(hh), cudaMemcpyDeviceToHost, s));
         ctx->sync();
         for (int b = 0; b < 64; ++b)
-            if (hh[b]) ctx->count("ws.generations.frontier_2^" + std::to_string(b), static_cast<double>(hh[b]));
+            if (hh[b]) {
+                const std::string c = "ws.generations.frontier_2^" + std::to_string(b);
+                ctx->count(c, static_cast<double>(hh[b]));
+                ctx->count(c + ".claim_ms", hh[64 + b] * 1e-6);
+                ctx->count(c + ".resolve_ms", hh[128 + b] * 1e-6);
+            }
     }
 
     KernelTimer kt_tables(ctx, "ws_tables");  // to the end of the stage
