@@ -371,11 +371,13 @@ __global__ void plateau_stats(const uint32_t* __restrict__ pid, const uint32_t* 
     }
 }
 
-// Plateau edges q -> p (crad strictly decreasing), deduplicated per voxel and per block;
-// count receives the number of edges, also those beyond cap (not written).
+// Plateau edges q -> p (crad strictly decreasing), deduplicated per block; count receives
+// the number of edges, also those beyond cap (not written). Each unordered voxel pair is
+// visited once, from the voxel of smaller index (the 13 forward offsets), and gives the edge
+// from the pair's higher-radius plateau to the lower one; the keys stay in registers.
 constexpr int kEdgeTable = 2048;  // shared-memory pair set of plateau_edges (power of two)
 
-__global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
+__global__ void __launch_bounds__(256, 4) plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
                               Grid g, size_t n, int d3q7, unsigned long long* __restrict__ count,
                               unsigned long long* __restrict__ edges, unsigned long long cap) {
     const unsigned lane = threadIdx.x & 31;
@@ -384,27 +386,36 @@ __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* 
     for (size_t base = static_cast<size_t>(blockIdx.x) * blockDim.x; base < n;
          base += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const size_t v = base + threadIdx.x;
-        uint32_t seen[26];
-        int ns = 0;
+        unsigned long long key[13];
+        bool has[13];
         const uint32_t p = v < n ? pid[v] : kNone;
-        if (p != kNone) {
-            const uint32_t r = crad[v];
-            int x, y, z;
-            g.coords(v, x, y, z);
-            for (int j = 0; j < 27; ++j) {
-                int dx, dy, dz;
-                if (!stencil_offset(j, d3q7, dx, dy, dz)) continue;
-                const int nx = x + dx, ny = y + dy, nz = z + dz;
-                if (!g.inside(nx, ny, nz)) continue;
-                const size_t w = g.idx(nx, ny, nz);
-                const uint32_t rw = crad[w];
-                if (rw == 0 || rw >= r) continue;
-                const uint32_t q = pid[w];
-                bool dup = false;
-                for (int i = 0; i < ns; ++i) dup |= seen[i] == q;
-                if (dup) continue;
-                seen[ns++] = q;
+        const uint32_t r = p != kNone ? crad[v] : 0u;
+        int x = 0, y = 0, z = 0;
+        if (p != kNone) g.coords(v, x, y, z);
+#pragma unroll
+        for (int k = 0; k < 13; ++k) {  // the forward offsets, as in uf_hook
+            int dx, dy, dz;
+            if (k < 4) {
+                dz = 0;
+                dx = (k == 0) ? 0 : 1;
+                dy = (k == 0) ? 1 : k - 2;
+            } else {
+                dz = 1;
+                dx = (k - 4) / 3 - 1;
+                dy = (k - 4) % 3 - 1;
             }
+            has[k] = false;
+            key[k] = 0;
+            if (p == kNone || (d3q7 && (dx != 0) + (dy != 0) + (dz != 0) > 1)) continue;
+            const int nx = x + dx, ny = y + dy, nz = z + dz;
+            if (!g.inside(nx, ny, nz)) continue;
+            const size_t w = g.idx(nx, ny, nz);
+            const uint32_t rw = crad[w];
+            if (rw == 0 || rw == r) continue;
+            const uint32_t q = pid[w];
+            key[k] = rw < r ? (static_cast<unsigned long long>(q) << 32) | p
+                            : (static_cast<unsigned long long>(p) << 32) | q;
+            has[k] = true;
         }
         {
             // Neighbouring voxels mostly report the same plateau pairs: keep the first copy
@@ -412,34 +423,37 @@ __global__ void plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* 
             // finds no free slot is kept too - the sort and unique that follow are exact).
             for (int i = threadIdx.x; i < kEdgeTable; i += blockDim.x) table[i] = ~0ull;
             __syncthreads();
-            int kept = 0;
-            for (int i = 0; i < ns; ++i) {
-                const unsigned long long key = (static_cast<unsigned long long>(seen[i]) << 32) | p;
-                unsigned h = static_cast<unsigned>((key * 0x9E3779B97F4A7C15ull) >> 40) & (kEdgeTable - 1);
-                bool fresh = true;
+            unsigned ns = 0;
+#pragma unroll
+            for (int k = 0; k < 13; ++k) {
+                if (!has[k]) continue;
+                unsigned h = static_cast<unsigned>((key[k] * 0x9E3779B97F4A7C15ull) >> 40) & (kEdgeTable - 1);
                 for (int probe = 0; probe < 8; ++probe, h = (h + 1) & (kEdgeTable - 1)) {
-                    const unsigned long long prev = atomicCAS(&table[h], ~0ull, key);
+                    const unsigned long long prev = atomicCAS(&table[h], ~0ull, key[k]);
                     if (prev == ~0ull) break;
-                    if (prev == key) {
-                        fresh = false;
+                    if (prev == key[k]) {
+                        has[k] = false;
                         break;
                     }
                 }
-                if (fresh) seen[kept++] = seen[i];
+                ns += has[k] ? 1u : 0u;
             }
             __syncthreads();
-            ns = kept;
             // one atomic per warp; lanes place their edges by a warp prefix sum
-            unsigned incl = static_cast<unsigned>(ns);
+            unsigned incl = ns;
             for (int o = 1; o < 32; o <<= 1) {
                 const unsigned t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
                 if (lane >= static_cast<unsigned>(o)) incl += t;
             }
             unsigned long long pos = 0;
             if (lane == 31 && incl) pos = atomicAdd(count, static_cast<unsigned long long>(incl));
-            pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + (incl - static_cast<unsigned>(ns));
-            for (int i = 0; i < ns; ++i)
-                if (pos + i < cap) edges[pos + i] = (static_cast<unsigned long long>(seen[i]) << 32) | p;
+            pos = __shfl_sync(0xFFFFFFFFu, pos, 31) + (incl - ns);
+#pragma unroll
+            for (int k = 0; k < 13; ++k)
+                if (has[k]) {
+                    if (pos < cap) edges[pos] = key[k];
+                    ++pos;
+                }
         }
     }
 }
@@ -490,7 +504,11 @@ struct PlateauSets {
     uint8_t* big;                // [L] 1: merged by the sort path
     uint32_t* heavy;             // local indices of high in-degree plateaus
     uint32_t* big_list;          // local indices of the sort-path plateaus
-    unsigned long long* info;    // [0] heavy, [1] big, [2] big elements, [3] expansion fill
+    unsigned long long* info;    // [0] heavy, [1] big, [2] big elements, [3] expansion fill,
+                                 // [4] fill of the medium unions' buffer
+    uint32_t* mtmp;              // sorted medium unions of the level, until level_write
+    unsigned long long mtmp_cap;
+    unsigned long long* mtoff;   // [L] position of plateau L's medium union in mtmp
 };
 
 __device__ __forceinline__ uint32_t warp_min_u32(uint32_t v) {
@@ -541,11 +559,108 @@ __device__ __forceinline__ int warp_small_union(const PlateauSets& st, unsigned 
     return __popc(mask);
 }
 
+// Medium unions: predecessors whose sizes add up to at most kMedSum elements but repeat the
+// same seeds (a plateau's in-edges mostly come from plateaus reached by the same pores). One
+// warp inserts every element into a hash set of its own in shared memory; when at most kMedCap
+// distinct elements remain, they are sorted in the warp and the union stays on this path
+// instead of the expand-and-sort path of the big sets.
+constexpr unsigned kMedSum = 8192;
+constexpr int kMedCap = 128;
+constexpr int kMedHash = 256;  // slots (power of two, twice kMedCap)
+
+struct MedBuf {
+    uint32_t table[kMedHash];
+    uint32_t sorted[kMedCap];
+    unsigned int count;
+};
+
+// Inserts the predecessors' elements and the seed into the warp's hash set; returns the
+// number of distinct elements, or -1 when there are more than kMedCap.
+__device__ __forceinline__ int warp_medium_insert(const PlateauSets& st, unsigned e0, unsigned e1, uint32_t seed,
+                                                  MedBuf& mb, unsigned lane) {
+    for (int i = lane; i < kMedHash; i += 32) mb.table[i] = kNone;
+    if (lane == 0) mb.count = 0;
+    __syncwarp();
+    bool over = false;
+    auto insert = [&](uint32_t x) {
+        unsigned h = (x * 2654435761u) >> (32 - 8);  // kMedHash = 2^8 slots
+        for (int probe = 0; probe < kMedHash; ++probe, h = (h + 1) & (kMedHash - 1)) {
+            const uint32_t prev = atomicCAS(&mb.table[h], kNone, x);
+            if (prev == x) return;
+            if (prev == kNone) {
+                if (atomicAdd(&mb.count, 1u) >= static_cast<unsigned>(kMedCap)) over = true;
+                return;
+            }
+        }
+        over = true;  // table full (only after more than kMedCap insertions)
+    };
+    for (unsigned e = e0 + lane; e < e1 && !over; e += 32) {
+        const uint32_t q = static_cast<uint32_t>(st.edges[e]);
+        const uint32_t len = st.slen[q];
+        const uint32_t* src = st.pool + st.soff[q];
+        for (uint32_t k = 0; k < len && !over; ++k) {
+            insert(src[k]);
+            // another lane may have passed the cap: stop early
+            if (*reinterpret_cast<volatile unsigned int*>(&mb.count) > static_cast<unsigned>(kMedCap)) over = true;
+        }
+    }
+    if (seed != kNone && lane == 0 && !over) insert(seed);
+    if (__any_sync(0xFFFFFFFFu, over)) return -1;
+    __syncwarp();
+    const unsigned n = mb.count;
+    return n > static_cast<unsigned>(kMedCap) ? -1 : static_cast<int>(n);
+}
+
+// The union gathered by warp_medium_insert (n elements), sorted ascending: up to 32 elements
+// in the lanes' registers, more in mb.sorted. Lane l then holds element l (value, keep = l < n)
+// when n <= 32.
+__device__ __forceinline__ void warp_medium_sort(MedBuf& mb, int n, unsigned lane, uint32_t& value) {
+    if (lane == 0) mb.count = 0;
+    __syncwarp();
+    for (int i = lane; i < kMedHash; i += 32) {
+        const uint32_t x = mb.table[i];
+        if (x != kNone) mb.sorted[atomicAdd(&mb.count, 1u)] = x;
+    }
+    __syncwarp();
+    if (n <= 32) {
+        uint32_t v = static_cast<int>(lane) < n ? mb.sorted[lane] : kNone;
+        for (int k = 2; k <= 32; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const uint32_t other = __shfl_xor_sync(0xFFFFFFFFu, v, j);
+                const bool ascending = (lane & k) == 0;
+                const bool lower = (lane & j) == 0;
+                v = (lower == ascending) ? min(v, other) : max(v, other);
+            }
+        value = v;
+        return;
+    }
+    int N = 64;
+    while (N < n) N <<= 1;
+    for (int i = n + lane; i < N; i += 32) mb.sorted[i] = kNone;
+    __syncwarp();
+    for (int k = 2; k <= N; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < N; i += 32) {
+                const int q = i ^ j;
+                if (q > i) {
+                    const uint32_t a = mb.sorted[i], b = mb.sorted[q];
+                    if (((i & k) == 0) ? (a > b) : (a < b)) {
+                        mb.sorted[i] = b;
+                        mb.sorted[q] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    value = kNone;
+}
+
 // Seeds, m and set sizes of one level, one warp per plateau. Small unions are counted here;
 // larger ones go to the sort path and plateaus with many in-edges to level_heavy.
 __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
     __shared__ uint32_t wbuf[kLevelWarps][kSmallSet];
     __shared__ unsigned int wfill[kLevelWarps];
+    __shared__ MedBuf med[kLevelWarps];
     const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const size_t stride = static_cast<size_t>(gridDim.x) * kLevelWarps;
     for (size_t i = begin + static_cast<size_t>(blockIdx.x) * kLevelWarps + w; i < end; i += stride) {
@@ -585,11 +700,36 @@ __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
                 st.big[L] = 0;
                 st.cnt[L] = static_cast<unsigned long long>(k);
             }
-        } else if (lane == 0) {
-            st.big[L] = 1;
-            st.cnt[L] = 0;
-            st.big_list[atomicAdd(&st.info[1], 1ull)] = static_cast<uint32_t>(L);
-            atomicAdd(&st.info[2], total);
+        } else {
+            int k = total <= kMedSum ? warp_medium_insert(st, e0, e1, seed, med[w], lane) : -1;
+            if (k >= 0) {  // a medium union: sorted now, kept in mtmp until level_write
+                uint32_t v;
+                warp_medium_sort(med[w], k, lane, v);
+                unsigned long long at = 0;
+                if (lane == 0) at = atomicAdd(&st.info[4], static_cast<unsigned long long>(k));
+                at = __shfl_sync(0xFFFFFFFFu, at, 0);
+                if (at + k <= st.mtmp_cap) {
+                    if (k <= 32) {
+                        if (static_cast<int>(lane) < k) st.mtmp[at + lane] = v;
+                    } else {
+                        for (int r = lane; r < k; r += 32) st.mtmp[at + r] = med[w].sorted[r];
+                    }
+                    if (lane == 0) st.mtoff[L] = at;
+                } else {
+                    k = -1;  // no room left: the sort path takes it
+                }
+            }
+            if (lane == 0) {
+                if (k >= 0) {
+                    st.big[L] = 2;
+                    st.cnt[L] = static_cast<unsigned long long>(k);
+                } else {
+                    st.big[L] = 1;
+                    st.cnt[L] = 0;
+                    st.big_list[atomicAdd(&st.info[1], 1ull)] = static_cast<uint32_t>(L);
+                    atomicAdd(&st.info[2], total);
+                }
+            }
         }
     }
 }
@@ -875,7 +1015,13 @@ __global__ void level_write(PlateauSets st, size_t begin, size_t end, const unsi
             st.slen[p] = fits ? static_cast<uint32_t>(k) : 0u;
             if (!fits) atomicOr(st.err, 2u);
         }
-        if (st.big[L]) continue;
+        if (st.big[L] == 1) continue;
+        if (st.big[L] == 2) {  // sorted by level_seeds
+            const uint32_t* src = st.mtmp + st.mtoff[L];
+            for (unsigned long long r = lane; r < k; r += 32)
+                if (fits) st.pool[pos + r] = src[r];
+            continue;
+        }
         uint32_t v;
         bool keep;
         int rank;
@@ -1277,7 +1423,11 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     ps.big = buf<uint8_t>(ctx, "pores.big", max_level);
     ps.heavy = buf<uint32_t>(ctx, "pores.heavy", max_level);
     ps.big_list = buf<uint32_t>(ctx, "pores.big_list", max_level);
-    ps.info = buf<unsigned long long>(ctx, "pores.info", 4);
+    ps.info = buf<unsigned long long>(ctx, "pores.info", 5);
+    ps.mtoff = buf<unsigned long long>(ctx, "pores.mtoff", max_level);
+    // medium unions of one level: a buffer of its own (a full buffer sends the rest to the sort path)
+    ps.mtmp_cap = std::min<unsigned long long>(std::max<unsigned long long>(1ull << 20, 8ull * np), 1ull << 26);
+    ps.mtmp = buf<uint32_t>(ctx, "pores.mtmp", ps.mtmp_cap);
     unsigned long long* base = reinterpret_cast<unsigned long long*>(d_count + 3);
     auto* h_info = static_cast<unsigned long long*>(ctx->host_staging(32));
     unsigned long long pool_cap = std::max<unsigned long long>(1ull << 22, 32ull * np);
@@ -1293,7 +1443,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         for (size_t l = 0; l + 1 < level_begin.size(); ++l) {
             const size_t b = level_begin[l], e = level_begin[l + 1];
             const unsigned lg = grid_for(ctx, (e - b) * 32, kLevelWarps * 32);
-            PMA_CUDA(cudaMemsetAsync(ps.info, 0, 32, s));
+            PMA_CUDA(cudaMemsetAsync(ps.info, 0, 40, s));
             {
                 KernelTimer kt2(ctx, "level_seeds");
                 level_seeds<<<lg, kLevelWarps * 32, 0, s>>>(ps, b, e);
