@@ -82,9 +82,9 @@ int pma_ctx_set_limits(pma_ctx* ctx, const pma_limits* limits);
  * to a renaming, 1 the reference's creation order (a host replay; see pma_pores). Batch and
  * server lanes created later inherit it. pma_run_folder always uses the reference's. */
 int pma_ctx_set_throat_numbering(pma_ctx* ctx, int reference_order);
-/* Runs one bounded device wait on a flag that nothing sets (the watershed's frontier
- * look-back waiting for a chunk that never publishes), with the context's spin_limit. Sets
- * *timed_out = 1 when the wait gave up and reported it, as it must. No counterpart in the
+/* Runs the bounded device waits on a flag that nothing sets (both forms of the watershed's
+ * frontier look-back waiting for a chunk that never publishes), with the context's spin_limit.
+ * Sets *timed_out = 1 when every wait gave up and reported it, as it must. No counterpart in the
  * reference; it exercises the error path of the device waits without faulting anything. */
 int pma_selftest_bounded_wait(pma_ctx* ctx, int* timed_out);
 

@@ -133,8 +133,12 @@ __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
 // lowers the neighbours it improves. Each voxel is in the list once, so a live entry
 // (bucket(dist) == k) is settled exactly once. Steps are in [1, 2), so pushes go to buckets
 // k + 1 and k + 2 only; they are counted per thread and added per warp at the end.
+// Four blocks per SM (64 registers; the float64 form spills about 100 bytes to L1): more
+// warps hide more of the neighbour loads' latency than the spilled registers cost (the float64
+// bucket loop of the 1024^3 spinodal: 338 ms at 120 registers, 299 ms at three blocks per SM,
+// 294 ms at four).
 template <class T, bool D3Q7>
-__global__ void __launch_bounds__(256) geo_bucket(Geo g, T w1, T w2, T w3, T* __restrict__ dist,
+__global__ void __launch_bounds__(256, 4) geo_bucket(Geo g, T w1, T w2, T w3, T* __restrict__ dist,
                                                   uint32_t* __restrict__ cavity, Frontier f, int k,
                                                   uint32_t cavity_id) {
     typedef typename Bits<T>::U U;

@@ -378,7 +378,7 @@ __global__ void plateau_stats(const uint32_t* __restrict__ pid, const uint32_t* 
 constexpr int kEdgeTable = 2048;  // shared-memory pair set of plateau_edges (power of two)
 
 __global__ void __launch_bounds__(256, 4) plateau_edges(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ crad,
-                              Grid g, size_t n, int d3q7, unsigned long long* __restrict__ count,
+                              Grid g, size_t n, int d3q7, int sb, unsigned long long* __restrict__ count,
                               unsigned long long* __restrict__ edges, unsigned long long cap) {
     const unsigned lane = threadIdx.x & 31;
     __shared__ unsigned long long table[kEdgeTable];
@@ -413,8 +413,8 @@ __global__ void __launch_bounds__(256, 4) plateau_edges(const uint32_t* __restri
             const uint32_t rw = crad[w];
             if (rw == 0 || rw == r) continue;
             const uint32_t q = pid[w];
-            key[k] = rw < r ? (static_cast<unsigned long long>(q) << 32) | p
-                            : (static_cast<unsigned long long>(p) << 32) | q;
+            key[k] = rw < r ? (static_cast<unsigned long long>(q) << sb) | p
+                            : (static_cast<unsigned long long>(p) << sb) | q;
             has[k] = true;
         }
         {
@@ -458,13 +458,15 @@ __global__ void __launch_bounds__(256, 4) plateau_edges(const uint32_t* __restri
     }
 }
 
-// CSR offsets of edges sorted by destination (key high word).
-__global__ void edge_offsets(const unsigned long long* __restrict__ edges, size_t ne, size_t np,
-                             unsigned int* __restrict__ eoff) {
+// CSR offsets of edges sorted by destination (key >> sb), and the sources (the low sb bits) as
+// 32-bit words, the form the level sweep reads.
+__global__ void edge_offsets(const unsigned long long* __restrict__ edges, size_t ne, size_t np, int sb,
+                             unsigned int* __restrict__ eoff, uint32_t* __restrict__ src) {
     PMA_GRID_STRIDE(i, ne + 1) {
-        const uint32_t cur = (i < ne) ? static_cast<uint32_t>(edges[i] >> 32) : static_cast<uint32_t>(np);
-        const uint32_t prev = (i == 0) ? 0u : static_cast<uint32_t>(edges[i - 1] >> 32) + 1u;
+        const uint32_t cur = (i < ne) ? static_cast<uint32_t>(edges[i] >> sb) : static_cast<uint32_t>(np);
+        const uint32_t prev = (i == 0) ? 0u : static_cast<uint32_t>(edges[i - 1] >> sb) + 1u;
         for (uint32_t p = prev; p <= cur && p <= np; ++p) eoff[p] = static_cast<unsigned int>(i);
+        if (i < ne) src[i] = static_cast<uint32_t>(edges[i] & ((1ull << sb) - 1));
     }
 }
 
@@ -488,7 +490,7 @@ constexpr int kLevelWarps = 4;           // warps per block of the per-plateau k
 // in `order` minus the level's first position).
 struct PlateauSets {
     const unsigned int* eoff;
-    const unsigned long long* edges;  // sorted by destination; low word = source
+    const uint32_t* edges;  // sources, sorted by destination
     const uint32_t* order;            // plateaus in decreasing crad
     const uint32_t* minrank;
     uint32_t* m;       // smallest ball rank reaching the plateau
@@ -567,6 +569,7 @@ __device__ __forceinline__ int warp_small_union(const PlateauSets& st, unsigned 
 constexpr unsigned kMedSum = 8192;
 constexpr int kMedCap = 128;
 constexpr int kMedHash = 256;  // slots (power of two, twice kMedCap)
+constexpr unsigned long long kMedSlab = 1024;  // buffer space a warp takes at a time
 
 struct MedBuf {
     uint32_t table[kMedHash];
@@ -662,6 +665,7 @@ __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
     __shared__ unsigned int wfill[kLevelWarps];
     __shared__ MedBuf med[kLevelWarps];
     const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long slab_base = 0, slab_left = 0;  // the warp's medium-union buffer space
     const size_t stride = static_cast<size_t>(gridDim.x) * kLevelWarps;
     for (size_t i = begin + static_cast<size_t>(blockIdx.x) * kLevelWarps + w; i < end; i += stride) {
         const size_t L = i - begin;
@@ -705,10 +709,18 @@ __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
             if (k >= 0) {  // a medium union: sorted now, kept in mtmp until level_write
                 uint32_t v;
                 warp_medium_sort(med[w], k, lane, v);
-                unsigned long long at = 0;
-                if (lane == 0) at = atomicAdd(&st.info[4], static_cast<unsigned long long>(k));
-                at = __shfl_sync(0xFFFFFFFFu, at, 0);
-                if (at + k <= st.mtmp_cap) {
+                // the warp takes buffer space in slabs of kMedSlab elements (one atomic per slab,
+                // not one per union on a counter every warp of the level shares)
+                if (static_cast<unsigned long long>(k) > slab_left) {
+                    unsigned long long b = 0;
+                    if (lane == 0) b = atomicAdd(&st.info[4], static_cast<unsigned long long>(kMedSlab));
+                    slab_base = __shfl_sync(0xFFFFFFFFu, b, 0);
+                    slab_left = slab_base + kMedSlab <= st.mtmp_cap ? kMedSlab : 0;
+                }
+                const unsigned long long at = slab_base;
+                if (static_cast<unsigned long long>(k) <= slab_left) {
+                    slab_base += k;
+                    slab_left -= k;
                     if (k <= 32) {
                         if (static_cast<int>(lane) < k) st.mtmp[at + lane] = v;
                     } else {
@@ -1319,6 +1331,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     kt_ids.reset();
     // Edges between plateaus, sorted by destination.
     auto kt_edges = std::make_unique<KernelTimer>(ctx, "plateau_edges");
+    int sb = 1;  // bits of a plateau id
+    while (sb < 32 && (1ull << sb) < static_cast<unsigned long long>(np)) ++sb;
     auto* ecount = reinterpret_cast<unsigned long long*>(d_count + 1);
     // One pass writes the edges into a buffer of at least n/8 entries, or of what an earlier
     // call needed (the edges kept after the per-block de-duplication are far fewer than the
@@ -1332,7 +1346,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemsetAsync(ecount, 0, 8, s));
         {
             KernelTimer kt(ctx, "edges_write");
-            plateau_edges<<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, ecount, edges_raw, ecap);
+            plateau_edges<<<G, 256, 0, s>>>(pid, crad2, g, n, d3q7, sb, ecount, edges_raw, ecap);
         }
         ctx->check_launch("plateau_edges");
         PMA_CUDA(cudaMemcpyAsync(&ne_kept, ecount, 8, cudaMemcpyDeviceToHost, s));
@@ -1341,17 +1355,19 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_REQUIRE(attempt < 3, PMA_ERR_INTERNAL, "pma_pores: plateau edge count did not settle");
         ecap = ne_kept + ne_kept / 8 + 1024;
     }
-    // Keys are (destination << 32 | source): sorting groups the predecessors of each plateau.
+    // Keys are (destination << sb | source): sorting groups the predecessors of each plateau.
     int64_t ne = 0;
     if (ne_kept) {
         auto* edges = buf<unsigned long long>(ctx, "pores.edges", ne_kept);
-        sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_kept));
+        sort_keys(ctx, edges_raw, edges, static_cast<int64_t>(ne_kept), 2 * sb);  // used bits only
         ne = unique(ctx, edges, edges_raw, static_cast<int64_t>(ne_kept), d_count);
     }
-    unsigned long long* by_dst = edges_raw;
+    ctx->count("pores.plateaus", static_cast<double>(np));
+    ctx->count("pores.plateau_edges", static_cast<double>(ne));
+    uint32_t* by_dst = buf<uint32_t>(ctx, "pores.esrc", std::max<int64_t>(ne, 1));
     unsigned int* eoff = buf<unsigned int>(ctx, "pores.eoff", np + 1);
     PMA_CUDA(cudaMemsetAsync(eoff, 0, (np + 1) * 4, s));
-    edge_offsets<<<grid_for(ctx, ne + 1), 256, 0, s>>>(by_dst, ne, np, eoff);
+    edge_offsets<<<grid_for(ctx, ne + 1), 256, 0, s>>>(edges_raw, ne, np, sb, eoff, by_dst);
     ctx->check_launch("edge_offsets");
     kt_edges.reset();
 
@@ -1426,7 +1442,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     ps.info = buf<unsigned long long>(ctx, "pores.info", 5);
     ps.mtoff = buf<unsigned long long>(ctx, "pores.mtoff", max_level);
     // medium unions of one level: a buffer of its own (a full buffer sends the rest to the sort path)
-    ps.mtmp_cap = std::min<unsigned long long>(std::max<unsigned long long>(1ull << 20, 8ull * np), 1ull << 26);
+    ps.mtmp_cap = std::min<unsigned long long>(std::max<unsigned long long>(1ull << 22, 16ull * np), 1ull << 27);
     ps.mtmp = buf<uint32_t>(ctx, "pores.mtmp", ps.mtmp_cap);
     unsigned long long* base = reinterpret_cast<unsigned long long*>(d_count + 3);
     auto* h_info = static_cast<unsigned long long*>(ctx->host_staging(32));

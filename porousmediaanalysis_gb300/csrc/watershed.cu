@@ -79,7 +79,8 @@ struct WsState {
     unsigned int* err;
     int spin_limit;               // polls of one wait on another block before giving up
     unsigned long long* gen_hist; // NULL, or per log2 of the frontier size: [c] generations,
-                                  // [64 + c] ns in claim phases, [128 + c] ns in resolve phases
+                                  // [64 + c] ns in claim phases, [128 + c] ns in resolve phases;
+                                  // [192], [193]: block 0's ns resolving events, scan + look-back
     int time_shift;               // bucket entry time = (generation << time_shift) | event
     uint8_t* ev_touch;            // per event slot: phase 0 touched an unclaimed voxel
     const unsigned long long* boff;  // bucket offsets
@@ -167,9 +168,16 @@ __device__ __forceinline__ uint32_t ws_follow(uint32_t* link, const WsState& s) 
     if (rec == 0) {
         rec = atomicCAS(link, 0u, kRecBusy);
         if (rec == 0) {
-            const uint32_t fresh = atomicAdd(s.ext_count, 1u) + 1;
-            if (fresh > s.ext_cap) {  // out of records: give the number back, flag a redo
-                atomicSub(s.ext_count, 1u);
+            // the warp's allocating lanes take their record numbers with one atomic (a single
+            // counter for every new shared voxel of the flood would serialise them)
+            const unsigned peers = __activemask();
+            const int leader = __ffs(peers) - 1;
+            const unsigned lane = threadIdx.x & 31;
+            unsigned first = 0;
+            if (static_cast<int>(lane) == leader) first = atomicAdd(s.ext_count, static_cast<unsigned>(__popc(peers)));
+            first = __shfl_sync(peers, first, leader);
+            const uint32_t fresh = first + __popc(peers & ((1u << lane) - 1u)) + 1;
+            if (fresh > s.ext_cap) {  // out of records: flag a redo with more
                 atomicExch(link, 0u);
                 atomicOr(s.err, 1u);
                 return 0;
@@ -278,7 +286,17 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
             np_out = pore;
             return true;
         }
-        const unsigned pos = atomicAdd(&s.bfill[r], 1u);
+        // lanes of the warp appending to the same depth take their slots with one atomic: a
+        // generation's claims of shallower voxels mostly go to a few depths, and one counter
+        // per depth would serialise them
+        const unsigned active = __activemask();
+        const unsigned peers = __match_any_sync(active, r);
+        const int leader = __ffs(peers) - 1;
+        const unsigned lane = threadIdx.x & 31;
+        unsigned first = 0;
+        if (static_cast<int>(lane) == leader) first = atomicAdd(&s.bfill[r], static_cast<unsigned>(__popc(peers)));
+        first = __shfl_sync(peers, first, leader);
+        const unsigned pos = first + __popc(peers & ((1u << lane) - 1u));
         const unsigned long long at = s.boff[r] + pos;
         s.ent_time[at] = (gen << s.time_shift) | seq;
         s.ent_val[at] = (static_cast<unsigned long long>(pore) << 32) | w;
@@ -293,7 +311,7 @@ __device__ __forceinline__ bool ws_resolve_event(const WsState& s, const uint32_
 // Ordered compaction of a generation's same-depth claims into the next frontier, in event
 // order, inside the resolve phase: each chunk of kChunk events (one block, four per thread)
 // ranks its claims, and its offset comes from a decoupled look-back over the chunks before it,
-// read 32 descriptors at a time by one warp. A descriptor holds (generation << 40) | state << 38
+// read 256 descriptors at a time by one warp. A descriptor holds (generation << 40) | state << 38
 // | count, state 1 = the chunk's own count, 2 = the inclusive prefix; one of an older
 // generation is not yet published. Chunks publish their own count before looking back and
 // every block of the cooperative grid is resident, so the look-back always ends; it is bounded
@@ -306,8 +324,10 @@ constexpr unsigned long long kDescOwn = 1ull << 38;
 constexpr unsigned long long kDescIncl = 2ull << 38;
 constexpr unsigned long long kDescVal = (1ull << 38) - 1;
 
-// Called by all 32 lanes of one warp; returns the exclusive prefix of chunk c.
-__device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned long long c, unsigned long long gen,
+// Called by all 32 lanes of one warp; returns the exclusive prefix of chunk c, reading 32
+// descriptors a poll. Used where chunks are dealt round-robin: its light polling leaves the L2 to
+// the blocks still resolving (a 256-wide poll made single-round generations 10-40 % slower).
+__device__ unsigned long long ws_lookback32(unsigned long long* desc, unsigned long long c, unsigned long long gen,
                                           unsigned long long own, unsigned int* err, int spin_limit,
                                           unsigned lane) {
     volatile unsigned long long* vd = desc;
@@ -346,11 +366,73 @@ __device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned lon
     return excl;
 }
 
+// Called by all 32 lanes of one warp; returns the exclusive prefix of range c. Each poll reads
+// kLookbackPer descriptors per lane (256 ranges, nearest first) and needs them published only
+// up to the nearest inclusive prefix, so a range far from its last inclusive predecessor
+// reaches it in a few polls instead of one per 32. Used once per block and generation by the
+// contiguous-range compaction.
+constexpr int kLookbackPer = 8;
+__device__ unsigned long long ws_lookback(unsigned long long* desc, unsigned long long c, unsigned long long gen,
+                                          unsigned long long own, unsigned int* err, int spin_limit,
+                                          unsigned lane) {
+    volatile unsigned long long* vd = desc;
+    const unsigned long long tg = gen << 40;
+    if (lane == 0) vd[c] = tg | (c == 0 ? kDescIncl : kDescOwn) | own;
+    if (c == 0) return 0;
+    __threadfence();
+    unsigned long long excl = 0;
+    long long top = static_cast<long long>(c) - 1;
+    int spins = 0;
+    while (true) {
+        // lane l holds chunks top - l * kLookbackPer - j; before chunk 0 reads as an inclusive
+        // zero (chunk 0 is always inclusive, so the walk stops there anyway)
+        unsigned long long d[kLookbackPer];
+#pragma unroll
+        for (int j = 0; j < kLookbackPer; ++j) {
+            const long long p = top - static_cast<long long>(lane) * kLookbackPer - j;
+            d[j] = p >= 0 ? vd[p] : (tg | kDescIncl);
+        }
+        int fi = kLookbackPer, fn = kLookbackPer;  // this lane's first inclusive / first unpublished
+#pragma unroll
+        for (int j = kLookbackPer - 1; j >= 0; --j) {
+            if ((d[j] >> 40) != gen) fn = j;
+            else if (d[j] & kDescIncl) fi = j;
+        }
+        const unsigned incl = __ballot_sync(0xFFFFFFFFu, fi < fn);
+        const unsigned gap = __ballot_sync(0xFFFFFFFFu, fn < fi);
+        const unsigned any = incl | gap;
+        const int stop = any ? __ffs(any) - 1 : 32;  // the lane that decides this poll
+        if (stop < 32 && ((gap >> stop) & 1u)) {     // a predecessor before the inclusive is unpublished
+            if (++spins > spin_limit) {
+                if (lane == 0) atomicOr(err, 16u);
+                break;
+            }
+            continue;
+        }
+        const int upto = static_cast<int>(lane) < stop ? kLookbackPer : (static_cast<int>(lane) == stop ? fi + 1 : 0);
+        unsigned long long v = 0;
+#pragma unroll
+        for (int j = 0; j < kLookbackPer; ++j)
+            if (j < upto) v += d[j] & kDescVal;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        excl += v;
+        if (stop < 32) break;
+        top -= 32 * kLookbackPer;
+    }
+    if (lane == 0) {
+        __threadfence();
+        vd[c] = tg | kDescIncl | (excl + own);
+    }
+    return excl;
+}
+
 // A look-back at a chunk descriptor that nothing publishes (chunk 0 of generation 0 while
-// chunk 1 of generation 1 waits for it): the bounded wait of the frontier compaction runs
-// out after spin_limit polls and sets err bit 16, the path a stalled generation would take.
+// chunk 1 of generation 1 waits for it): each bounded wait of the frontier compaction (the
+// 32-wide one in err[0], the 256-wide one in err[1]) runs out after spin_limit polls and sets
+// bit 16, the path a stalled generation would take.
 __global__ void ws_wait_selftest(unsigned long long* desc, unsigned int* err, int spin_limit) {
-    ws_lookback(desc, 1, 1, 0, err, spin_limit, threadIdx.x & 31);
+    ws_lookback32(desc, 1, 1, 0, err, spin_limit, threadIdx.x & 31);
+    ws_lookback(desc, 1, 1, 0, err + 1, spin_limit, threadIdx.x & 31);
 }
 
 __device__ __forceinline__ unsigned long long ws_clock() {  // ns
@@ -396,10 +478,97 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
             atomicAdd(&s.gen_hist[64 + hc], t - t_start);
             t_start = t;
         }
+        const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
+        if (nchunks > gridDim.x) {
+            // More events than one round of chunks: each block resolves one contiguous range of
+            // events (each warp a contiguous part of it, 32 events a step) and counts its
+            // same-depth claims, marking them in ev_touch; one look-back per block gives its
+            // offset, and a second sweep over the range writes the marked claims in event order.
+            // (Chunks dealt round-robin would wait, round after round, for the slowest of their
+            // predecessors in the previous round.)
+            const bool probe = s.gen_hist && blockIdx.x == 0 && threadIdx.x == 0;
+            const unsigned long long ta = probe ? ws_clock() : 0;
+            const unsigned nwarp = blockDim.x >> 5;
+            const unsigned long long steps = (nev + 31) / 32;
+            const unsigned long long per_block = (steps + gridDim.x - 1) / gridDim.x;
+            const unsigned long long used = (steps + per_block - 1) / per_block;  // blocks with events
+            const unsigned long long per_warp = (per_block + nwarp - 1) / nwarp;
+            const unsigned long long b0 = blockIdx.x * per_block;
+            const unsigned long long b1 = min(b0 + per_block, steps);
+            const unsigned long long w0 = min(b0 + warp * per_warp, b1);
+            const unsigned long long w1 = min(w0 + per_warp, b1);
+            if (blockIdx.x < used) {
+                unsigned cnt = 0;
+                for (unsigned long long st = w0; st < w1; ++st) {
+                    const unsigned long long seq = st * 32 + lane;
+                    uint32_t wv, wp;
+                    const bool f = seq < nev && ws_resolve_event(s, gv, gp, seq, depth, gen, wv, wp);
+                    if (f) s.ev_touch[seq] = 2;
+                    cnt += __popc(__ballot_sync(0xFFFFFFFFu, f));
+                }
+                if (lane == 0) part[warp] = cnt;
+                __syncthreads();
+                const unsigned long long tb = probe ? ws_clock() : 0;
+                if (warp == 0) {
+                    const unsigned v = lane < nwarp ? part[lane] : 0u;
+                    unsigned incl = v;
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const unsigned t2 = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                        if (lane >= static_cast<unsigned>(o)) incl += t2;
+                    }
+                    const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                    if (lane < nwarp) part[lane] = incl - v;
+                    const unsigned long long base = ws_lookback(desc, blockIdx.x, gen, total, s.err, s.spin_limit, lane);
+                    if (lane == 0) {
+                        part[32] = static_cast<unsigned int>(base);
+                        if (blockIdx.x == used - 1) ng[cur ^ 1] = static_cast<unsigned int>(base + total);
+                    }
+                }
+                __syncthreads();
+                if (probe) {
+                    const unsigned long long tc = ws_clock();
+                    atomicAdd(&s.gen_hist[192], tb - ta);
+                    atomicAdd(&s.gen_hist[193], tc - tb);
+                }
+                unsigned long long pos = static_cast<unsigned long long>(part[32]) + part[warp];
+                // four steps at a time, every load issued before the stores
+                for (unsigned long long st = w0; st < w1; st += 4) {
+                    bool f[4];
+                    uint32_t v[4], pr[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const unsigned long long seq = (st + k) * 32 + lane;
+                        f[k] = st + k < w1 && seq < nev && __ldcg(s.ev_touch + seq) == 2;  // L2: no stale L1 line
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const unsigned long long i = ((st + k) * 32 + lane) / 27;
+                        v[k] = f[k] ? __ldcg(gv + i) : 0u;
+                        pr[k] = f[k] ? __ldcg(gp + i) : 0u;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const unsigned m = __ballot_sync(0xFFFFFFFFu, f[k]);
+                        if (f[k]) {
+                            const unsigned long long seq = (st + k) * 32 + lane;
+                            const int j = static_cast<int>(seq - seq / 27 * 27);
+                            int dx, dy, dz;
+                            stencil_offset(j, s.d3q7, dx, dy, dz);
+                            const unsigned long long at = pos + __popc(m & lt);
+                            nv[at] = static_cast<uint32_t>(static_cast<long long>(v[k]) +
+                                                           (static_cast<long long>(dz) * s.g.SX + dx) * s.g.SY + dy);
+                            np_[at] = pr[k];
+                        }
+                        pos += __popc(m);
+                    }
+                }
+            }
+        } else
         // Resolve by chunks of kChunk events: event k * blockDim + t of a chunk is thread t's
         // k-th, so event order is k-major, then thread.
-        const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
         for (unsigned long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
+            const bool probe = s.gen_hist && blockIdx.x == 0 && threadIdx.x == 0;  // block 0's split
+            const unsigned long long ta = probe ? ws_clock() : 0;
             bool f[4];
             uint32_t wv[4], wp[4];
             unsigned m[4];
@@ -411,6 +580,7 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
                 if (lane == 0) part[k * (kChunk / 128) + warp] = __popc(m[k]);
             }
             __syncthreads();
+            const unsigned long long tb = probe ? ws_clock() : 0;
             if (warp == 0) {  // 4 rounds x 8 warps = 32 counts in event order
                 const unsigned v = part[lane];
                 unsigned incl = v;
@@ -420,13 +590,18 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
                 }
                 const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
                 part[lane] = incl - v;
-                const unsigned long long base = ws_lookback(desc, c, gen, total, s.err, s.spin_limit, lane);
+                const unsigned long long base = ws_lookback32(desc, c, gen, total, s.err, s.spin_limit, lane);
                 if (lane == 0) {
                     part[32] = static_cast<unsigned int>(base);
                     if (c == nchunks - 1) ng[cur ^ 1] = static_cast<unsigned int>(base + total);
                 }
             }
             __syncthreads();
+            if (probe) {
+                const unsigned long long tc = ws_clock();
+                atomicAdd(&s.gen_hist[192], tb - ta);  // events resolved
+                atomicAdd(&s.gen_hist[193], tc - tb);  // scan and look-back
+            }
             const unsigned base = part[32];
 #pragma unroll
             for (int k = 0; k < 4; ++k)
@@ -734,8 +909,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     ws.spin_limit = ctx->limits.spin_limit;
     ws.gen_hist = nullptr;
     if (ctx->timing) {  // frontier sizes of the generations, for the timing report
-        ws.gen_hist = buf<unsigned long long>(ctx, "ws.gen_hist", 192);
-        PMA_CUDA(cudaMemsetAsync(ws.gen_hist, 0, 192 * 8, s));
+        ws.gen_hist = buf<unsigned long long>(ctx, "ws.gen_hist", 194);
+        PMA_CUDA(cudaMemsetAsync(ws.gen_hist, 0, 194 * 8, s));
     }
     ws.pbound = buf<unsigned int>(ctx, "ws.pbound", npores);
     // Shared-voxel records: a first guess of n/32; the pool doubles (copying the records)
@@ -939,7 +1114,7 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     PMA_REQUIRE(!(h_err & 8u), PMA_ERR_LIMIT, "pma_watershed: shared-voxel record allocation did not finish");
     PMA_REQUIRE(!(h_err & 16u), PMA_ERR_LIMIT, "pma_watershed: frontier compaction look-back did not finish");
     if (ws.gen_hist) {
-        unsigned long long hh[192];
+        unsigned long long hh[194];
         PMA_CUDA(cudaMemcpyAsync(hh, ws.gen_hist, sizeof(hh), cudaMemcpyDeviceToHost, s));
         ctx->sync();
         for (int b = 0; b < 64; ++b)
@@ -949,6 +1124,8 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
                 ctx->count(c + ".claim_ms", hh[64 + b] * 1e-6);
                 ctx->count(c + ".resolve_ms", hh[128 + b] * 1e-6);
             }
+        ctx->count("ws.block0.resolve_events_ms", hh[192] * 1e-6);
+        ctx->count("ws.block0.scan_lookback_ms", hh[193] * 1e-6);
     }
 
     KernelTimer kt_tables(ctx, "ws_tables");  // to the end of the stage
@@ -1087,10 +1264,10 @@ void wait_selftest(pma_ctx* ctx, int* timed_out) {
     ws_wait_selftest<<<1, 32, 0, ctx->stream>>>(desc, err, ctx->limits.spin_limit);
     ctx->count_launch();
     ctx->check_launch("ws_wait_selftest");
-    unsigned int h = 0;
-    PMA_CUDA(cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned int h[2] = {0, 0};
+    PMA_CUDA(cudaMemcpyAsync(h, err, 8, cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
-    *timed_out = (h & 16u) ? 1 : 0;
+    *timed_out = (h[0] & h[1] & 16u) ? 1 : 0;
 }
 
 }  // namespace pma
