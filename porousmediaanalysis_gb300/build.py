@@ -16,7 +16,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 LIB_SOURCES = ["capi.cpp", "pipeline.cpp", "batch.cpp", "serve.cpp", "pma_io.cpp", "exact_ids.cpp", "edt.cu",
-               "balls.cu", "geodesic.cu", "pores.cu", "watershed.cu", "resample.cu"]
+               "balls.cu", "geodesic.cu", "pores.cu", "watershed.cu", "resample.cu", "transfer.cu"]
 LIB = os.path.join(OUT, "libpma.so")
 CLI = os.path.join(OUT, "pma")
 

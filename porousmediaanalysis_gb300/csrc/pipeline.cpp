@@ -54,8 +54,8 @@ Fields alloc_fields(pma_ctx* ctx, size_t n, bool pores, bool geo, bool geo64) {
 }
 
 template <class T>
-void d2h(cudaStream_t s, T* host, const T* dev, size_t n) {
-    if (host && dev) PMA_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+void d2h(pma_ctx* ctx, T* host, const T* dev, size_t n) {
+    if (host && dev) copy_to_host(ctx, host, dev, n * sizeof(T));
 }
 
 }  // namespace
@@ -102,27 +102,26 @@ void run_pipeline_host(pma_ctx* ctx, const uint8_t* h_solid, pma_dims dims, cons
     const bool geo64 = o.run_geodesic && o.geodesic_fp64;
     Fields f = alloc_fields(ctx, n, o.run_pores != 0, o.run_geodesic != 0 && !geo64, geo64);
     if (geo64) f.cavity = static_cast<uint32_t*>(ctx->scratch("pipe.cavity", n * 4));
-    PMA_CUDA(cudaMemcpyAsync(f.solid, h_solid, n, cudaMemcpyHostToDevice, ctx->stream));
+    copy_from_host(ctx, f.solid, h_solid, n);
     run_pore_chain(ctx, f, dims, o, out);
     run_geo_chain(ctx, f, dims, o, out);
-    // Results go back after the whole chain. (Copying the pore-stage fields on a second
-    // stream while the geodesics ran made the geodesic kernels slower, 337 -> 754 ms at 1024^3,
-    // by more than the copy itself costs: the copy into the caller's pinned buffer and the
-    // geodesics' random accesses compete for address translation.)
+    // Results go back after the whole chain. (Copying the pore-stage fields with the copy
+    // engine on a second stream while the geodesics ran made the geodesic kernels slower,
+    // 337 -> 754 ms at 1024^3, by more than the copy itself costs.)
     if (o.run_pores) {
-        d2h(ctx->stream, out->edt2, f.edt2, n);
-        d2h(ctx->stream, out->crad2, f.crad2, n);
-        d2h(ctx->stream, out->cx, f.cx, n);
-        d2h(ctx->stream, out->cy, f.cy, n);
-        d2h(ctx->stream, out->cz, f.cz, n);
-        d2h(ctx->stream, out->maxball_mask, f.mask, n);
-        d2h(ctx->stream, out->pore_labels, f.labels, n);
-        d2h(ctx->stream, out->watershed_labels, f.labels_ws, n);
+        d2h(ctx, out->edt2, f.edt2, n);
+        d2h(ctx, out->crad2, f.crad2, n);
+        d2h(ctx, out->cx, f.cx, n);
+        d2h(ctx, out->cy, f.cy, n);
+        d2h(ctx, out->cz, f.cz, n);
+        d2h(ctx, out->maxball_mask, f.mask, n);
+        d2h(ctx, out->pore_labels, f.labels, n);
+        d2h(ctx, out->watershed_labels, f.labels_ws, n);
     }
     if (o.run_geodesic) {
-        d2h(ctx->stream, out->dist_f32, f.dist32, n);
-        d2h(ctx->stream, out->dist_f64, f.dist64, n);
-        d2h(ctx->stream, out->cavity, f.cavity, n);
+        d2h(ctx, out->dist_f32, f.dist32, n);
+        d2h(ctx, out->dist_f64, f.dist64, n);
+        d2h(ctx, out->cavity, f.cavity, n);
     }
     ctx->sync();
 }

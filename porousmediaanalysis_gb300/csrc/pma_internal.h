@@ -171,6 +171,10 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
 pma_table* watershed(pma_ctx* ctx, const pma_table* pores, const uint32_t* crad2, pma_dims d,
                      pma_stencil st, uint32_t max_edt2, uint32_t* labels);
 void wait_selftest(pma_ctx* ctx, int* timed_out);
+// Whole-field transfers on the context's stream: a streaming kernel through the mapped address
+// of a page-locked host buffer, cudaMemcpyAsync for pageable ones (transfer.cu).
+void copy_to_host(pma_ctx* ctx, void* host, const void* dev, size_t bytes);
+void copy_from_host(pma_ctx* ctx, void* dev, const void* host, size_t bytes);
 // resample.cu: 8-bit slices [nz][sx][sy] (host) upsampled in plane to [nz][dx][dy] as the
 // reference's image rescale does.
 std::vector<uint8_t> resample_slices(pma_ctx* ctx, const std::vector<uint8_t>& src, int nz, int sx, int sy, int dx,

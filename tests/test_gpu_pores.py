@@ -95,6 +95,36 @@ def test_pipeline_host_matches_stage_calls(ctx, ref_cases):
     assert res["watershed"].rows() == (rows(rec["pores_ws"]), rows(rec["throats_ws"]))
 
 
+def test_pipeline_host_with_page_locked_buffers(ctx):
+    """Page-locked host buffers move through the streaming copy kernel (16-byte words plus a
+    tail of 4 to 13 bytes on this odd-sized volume), a buffer offset by 4 bytes through the copy
+    engine: every field equals the run on pageable buffers."""
+    import numpy as np
+    import torch
+    import porousmediaanalysis_gb300 as pma
+    vol, _ = make_case("pack_odd")
+    fields = ("edt2", "crad2", "cx", "cy", "cz", "maxball_mask", "pore_labels", "watershed_labels",
+              "dist_f64", "cavity")
+    plain = pma.pipeline_host(ctx, vol, fp64=True, fields=fields)
+    kinds = {"maxball_mask": (torch.uint8, np.uint8), "dist_f64": (torch.float64, np.float64)}
+    pinned_in = torch.from_numpy(vol).pin_memory()
+    keep, outs = [], {}
+    for name in fields:
+        tdt, ndt = kinds.get(name, (torch.int32, np.uint32))
+        if name == "cx":  # a view 4 bytes into its pinned block: alignments differ
+            blk = torch.empty(vol.size + 1, dtype=torch.int32).pin_memory()
+            arr = blk.numpy()[1:].view(np.uint32).reshape(vol.shape)
+        else:
+            blk = torch.empty(vol.shape, dtype=tdt).pin_memory()
+            arr = blk.numpy().view(ndt)
+        keep.append(blk)
+        outs[name] = arr
+    res = pma.pipeline_host(ctx, pinned_in.numpy(), fp64=True, fields=fields, out_arrays=outs)
+    for name in fields:
+        assert np.array_equal(res[name], plain[name]), name
+    assert res["watershed"].rows() == plain["watershed"].rows()
+
+
 def test_watershed_accepts_pores_read_back(ctx, ref_cases):
     """Pores built from table rows (as read from pores.txt) drive the watershed."""
     import torch
