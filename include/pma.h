@@ -222,7 +222,10 @@ int pma_geodesic_f64(pma_ctx* ctx, const uint8_t* d_solid, pma_dims dims, pma_st
 /* ---------------------------------------------------------------------------------
  * Whole pipeline on one volume, host buffers in and out (EDT -> containing balls ->
  * pores -> empty-pore removal -> watershed, plus geodesics), the host<->device copies
- * included. Any output pointer may be NULL to skip copying that field back.
+ * included. Any output pointer may be NULL to skip copying that field back. Page-locked
+ * buffers (cudaHostAlloc, cudaHostRegister) are read and written by a streaming kernel
+ * through their mapped address, at the link's full rate; pageable ones through
+ * cudaMemcpyAsync.
  * ------------------------------------------------------------------------------- */
 typedef struct pma_outputs {
     uint32_t* edt2;             /* EuclideanDistanceSquares */

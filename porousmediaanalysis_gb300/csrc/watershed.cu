@@ -479,13 +479,15 @@ __global__ void __launch_bounds__(kChunk / 4, 4) ws_generations(WsState s, uint3
             t_start = t;
         }
         const unsigned long long nchunks = (nev + kChunk - 1) / kChunk;
-        if (nchunks > gridDim.x) {
-            // More events than one round of chunks: each block resolves one contiguous range of
+        if (nchunks > 8ull * gridDim.x) {
+            // More than eight rounds of chunks: each block resolves one contiguous range of
             // events (each warp a contiguous part of it, 32 events a step) and counts its
             // same-depth claims, marking them in ev_touch; one look-back per block gives its
             // offset, and a second sweep over the range writes the marked claims in event order.
-            // (Chunks dealt round-robin would wait, round after round, for the slowest of their
-            // predecessors in the previous round.)
+            // (Chunks dealt round-robin wait, round after round, for the slowest of their
+            // predecessors in the previous round: at 1024^3, 720 against 837 us per generation
+            // of 2^20 nodes; with fewer rounds the extra sweep costs more than it saves. Issuing
+            // each thread's loads of several events together did not pay in either phase.)
             const bool probe = s.gen_hist && blockIdx.x == 0 && threadIdx.x == 0;
             const unsigned long long ta = probe ? ws_clock() : 0;
             const unsigned nwarp = blockDim.x >> 5;
