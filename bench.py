@@ -47,8 +47,8 @@ WORKLOADS = {
 # DRAM bytes per voxel measured by ncu over all launches of a kernel in one step of a 320^3
 # GRF, used as the roofline's `traffic` when that kernel dominates.
 TRAFFIC_PER_VOXEL = {
-    "ws_generations": (268.0, "ncu dram__bytes_read+write of all ws_generations launches of one 320^3 "
-                              "GRF step, scaled by voxels"),
+    "ws_generations": (156.2, "ncu dram__bytes_read+write of the 107 ws_generations launches of one "
+                              "320^3 GRF step (4683 MB read, 436 MB written), scaled by voxels"),
 }
 
 # Algorithmic HBM bytes per voxel of the timed kernels (reads + writes each kernel must do).

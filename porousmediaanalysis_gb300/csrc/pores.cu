@@ -490,6 +490,10 @@ constexpr int kLevelWarps = 4;           // warps per block of the per-plateau k
 // in `order` minus the level's first position).
 struct PlateauSets {
     const unsigned int* eoff;
+    // Read-only path: the edges, and every array entry of a predecessor (m, slen, soff, its
+    // pool elements), are read through __ldg. A predecessor has a larger radius, so it belongs
+    // to an earlier level and was written by an earlier launch; the loads need not wait for
+    // the launch's own stores to the sweep's 32-bit arrays.
     const uint32_t* edges;  // sources, sorted by destination
     const uint32_t* order;            // plateaus in decreasing crad
     const uint32_t* minrank;
@@ -532,13 +536,13 @@ __device__ __forceinline__ int warp_small_union(const PlateauSets& st, unsigned 
     if (lane == 0) *wfill = 0;
     __syncwarp();
     for (unsigned e = e0 + lane; e < e1; e += 32) {
-        const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-        const uint32_t len = st.slen[q];
+        const uint32_t q = __ldg(st.edges + e);
+        const uint32_t len = __ldg(st.slen + q);
         if (!len) continue;
         const unsigned pos = atomicAdd(wfill, len);
-        const uint32_t* src = st.pool + st.soff[q];
+        const uint32_t* src = st.pool + __ldg(st.soff + q);
         for (uint32_t k = 0; k < len; ++k)
-            if (pos + k < kSmallSet) wbuf[pos + k] = src[k];
+            if (pos + k < kSmallSet) wbuf[pos + k] = __ldg(src + k);
     }
     __syncwarp();
     const unsigned total = min(*wfill, static_cast<unsigned>(kSmallSet));
@@ -598,11 +602,11 @@ __device__ __forceinline__ int warp_medium_insert(const PlateauSets& st, unsigne
         over = true;  // table full (only after more than kMedCap insertions)
     };
     for (unsigned e = e0 + lane; e < e1 && !over; e += 32) {
-        const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-        const uint32_t len = st.slen[q];
-        const uint32_t* src = st.pool + st.soff[q];
+        const uint32_t q = __ldg(st.edges + e);
+        const uint32_t len = __ldg(st.slen + q);
+        const uint32_t* src = st.pool + __ldg(st.soff + q);
         for (uint32_t k = 0; k < len && !over; ++k) {
-            insert(src[k]);
+            insert(__ldg(src + k));
             // another lane may have passed the cap: stop early
             if (*reinterpret_cast<volatile unsigned int*>(&mb.count) > static_cast<unsigned>(kMedCap)) over = true;
         }
@@ -682,9 +686,9 @@ __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
         uint32_t mp = kNone;
         unsigned long long u = 0;
         for (unsigned e = e0 + lane; e < e1; e += 32) {
-            const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-            mp = min(mp, st.m[q]);
-            u += st.slen[q];
+            const uint32_t q = __ldg(st.edges + e);
+            mp = min(mp, __ldg(st.m + q));
+            u += __ldg(st.slen + q);
         }
         mp = warp_min_u32(mp);
         u = warp_sum_u64(u);
@@ -759,9 +763,9 @@ __global__ void level_heavy(PlateauSets st, size_t begin) {
         uint32_t mp = kNone;
         unsigned long long u = 0;
         for (unsigned e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-            const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-            mp = min(mp, st.m[q]);
-            u += st.slen[q];
+            const uint32_t q = __ldg(st.edges + e);
+            mp = min(mp, __ldg(st.m + q));
+            u += __ldg(st.slen + q);
         }
         mp = warp_min_u32(mp);
         u = warp_sum_u64(u);
@@ -842,9 +846,9 @@ __global__ void __launch_bounds__(256) level_expand(PlateauSets st, size_t begin
             }
             const uint32_t L = st.big_list[lo];
             const uint32_t p = st.order[begin + L];
-            const uint32_t q = static_cast<uint32_t>(st.edges[st.eoff[p] + (t - doff[lo])]);
-            len = st.slen[q];
-            src = st.pool + st.soff[q];
+            const uint32_t q = __ldg(st.edges + st.eoff[p] + (t - doff[lo]));
+            len = __ldg(st.slen + q);
+            src = st.pool + __ldg(st.soff + q);
             hi = static_cast<K>(lo) << shift;
         }
         // The warp's 32 sets are expanded together, 32 elements per round: element u of the
@@ -871,7 +875,7 @@ __global__ void __launch_bounds__(256) level_expand(PlateauSets st, size_t begin
             K key = 0;
             bool emit = false;
             if (u < wtotal) {
-                key = ohi | static_cast<K>(osrc[u - oexcl]);
+                key = ohi | static_cast<K>(__ldg(osrc + (u - oexcl)));
                 emit = true;
                 unsigned h = static_cast<unsigned>((static_cast<unsigned long long>(key) * 0x9E3779B97F4A7C15ull) >> 40) &
                              (kMergeTable - 1);
@@ -937,12 +941,12 @@ __global__ void __launch_bounds__(1024) level_merge_small(PlateauSets st, size_t
         const unsigned e0 = st.eoff[p], e1 = st.eoff[p + 1];
         const unsigned long long hi = static_cast<unsigned long long>(b) << 32;
         for (unsigned e = e0 + lane; e < e1; e += 32) {
-            const uint32_t q = static_cast<uint32_t>(st.edges[e]);
-            const uint32_t len = st.slen[q];
-            const uint32_t* src = st.pool + st.soff[q];
+            const uint32_t q = __ldg(st.edges + e);
+            const uint32_t len = __ldg(st.slen + q);
+            const uint32_t* src = st.pool + __ldg(st.soff + q);
             const unsigned pos = atomicAdd(&s_count, len);
             for (uint32_t k = 0; k < len; ++k)
-                if (pos + k < kSmallMerge) sk[pos + k] = hi | src[k];
+                if (pos + k < kSmallMerge) sk[pos + k] = hi | __ldg(src + k);
         }
         if (lane == 0 && st.seed[p] != kNone) {
             const unsigned pos = atomicAdd(&s_count, 1u);
@@ -1256,9 +1260,14 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             if (t.joinable()) t.join();
         }
     } sorter;
-    sorter.t = std::thread([&items] {
-        ordered_sort(items.begin(), items.end(),
-                     [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); });
+    // up to 16 leaf tasks (levels 4) where the host has the cores: the leaves' sorts are most
+    // of the time, the top partition steps run on one to eight threads
+    int sort_levels = 1;
+    while (sort_levels < 4 && (2u << sort_levels) <= std::thread::hardware_concurrency()) ++sort_levels;
+    sorter.t = std::thread([&items, sort_levels] {
+        ordered_sort(
+            items.begin(), items.end(),
+            [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); }, sort_levels);
     });
 
     // Plateaus: connected sets of equal crad under the stencil.
@@ -1456,8 +1465,13 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         PMA_CUDA(cudaMemsetAsync(base, 0, 8, s));
         PMA_CUDA(cudaMemsetAsync(err, 0, 4, s));
         KernelTimer kt(ctx, "level_sets");
+        // per size class of the levels (plateaus in the level, log2), when timing is on
+        static const char* const kLevelClass[32] = {"levels.plateaus_2^0", "levels.plateaus_2^1", "levels.plateaus_2^2", "levels.plateaus_2^3", "levels.plateaus_2^4", "levels.plateaus_2^5", "levels.plateaus_2^6", "levels.plateaus_2^7", "levels.plateaus_2^8", "levels.plateaus_2^9", "levels.plateaus_2^10", "levels.plateaus_2^11", "levels.plateaus_2^12", "levels.plateaus_2^13", "levels.plateaus_2^14", "levels.plateaus_2^15", "levels.plateaus_2^16", "levels.plateaus_2^17", "levels.plateaus_2^18", "levels.plateaus_2^19", "levels.plateaus_2^20", "levels.plateaus_2^21", "levels.plateaus_2^22", "levels.plateaus_2^23", "levels.plateaus_2^24", "levels.plateaus_2^25", "levels.plateaus_2^26", "levels.plateaus_2^27", "levels.plateaus_2^28", "levels.plateaus_2^29", "levels.plateaus_2^30", "levels.plateaus_2^31"};
         for (size_t l = 0; l + 1 < level_begin.size(); ++l) {
             const size_t b = level_begin[l], e = level_begin[l + 1];
+            int lclass = 0;
+            while (lclass < 31 && (2ull << lclass) <= e - b) ++lclass;
+            KernelTimer kt_level(ctx, kLevelClass[lclass]);
             const unsigned lg = grid_for(ctx, (e - b) * 32, kLevelWarps * 32);
             PMA_CUDA(cudaMemsetAsync(ps.info, 0, 40, s));
             {
