@@ -662,14 +662,31 @@ __device__ __forceinline__ void warp_medium_sort(MedBuf& mb, int n, unsigned lan
     value = kNone;
 }
 
-// Seeds, m and set sizes of one level, one warp per plateau. Small unions are counted here;
-// larger ones go to the sort path and plateaus with many in-edges to level_heavy.
-__global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
+// Seeds, m and set sizes of one level, one warp per plateau. Small and medium unions are
+// merged here and kept, sorted, in mtmp until level_write copies them to the pool; larger ones
+// go to the sort path and plateaus with many in-edges to level_heavy. A union that finds no
+// room in mtmp is merged again by level_write (small) or takes the sort path (medium).
+__global__ void level_seeds(PlateauSets st, size_t begin, size_t end, unsigned slab) {
     __shared__ uint32_t wbuf[kLevelWarps][kSmallSet];
     __shared__ unsigned int wfill[kLevelWarps];
     __shared__ MedBuf med[kLevelWarps];
     const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    unsigned long long slab_base = 0, slab_left = 0;  // the warp's medium-union buffer space
+    // The warp takes mtmp space in slabs (one atomic per slab, not one per union on a counter
+    // every warp of the level shares); returns the start of k elements, or ~0 when full.
+    unsigned long long slab_base = 0, slab_left = 0;
+    auto take = [&](unsigned long long k) -> unsigned long long {
+        if (k > slab_left) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&st.info[4], static_cast<unsigned long long>(slab));
+            slab_base = __shfl_sync(0xFFFFFFFFu, b, 0);
+            slab_left = slab_base + slab <= st.mtmp_cap ? slab : 0;
+        }
+        if (k > slab_left) return ~0ull;
+        const unsigned long long at = slab_base;
+        slab_base += k;
+        slab_left -= k;
+        return at;
+    };
     const size_t stride = static_cast<size_t>(gridDim.x) * kLevelWarps;
     for (size_t i = begin + static_cast<size_t>(blockIdx.x) * kLevelWarps + w; i < end; i += stride) {
         const size_t L = i - begin;
@@ -704,8 +721,13 @@ __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
             bool keep;
             int rank;
             const int k = warp_small_union(st, e0, e1, seed, wbuf[w], &wfill[w], lane, v, keep, rank);
+            const unsigned long long at = k > 0 ? take(static_cast<unsigned long long>(k)) : 0ull;
+            if (at != ~0ull) {
+                if (keep) st.mtmp[at + rank] = v;
+                if (lane == 0) st.mtoff[L] = at;
+            }
             if (lane == 0) {
-                st.big[L] = 0;
+                st.big[L] = at != ~0ull ? 2 : 0;
                 st.cnt[L] = static_cast<unsigned long long>(k);
             }
         } else {
@@ -713,18 +735,8 @@ __global__ void level_seeds(PlateauSets st, size_t begin, size_t end) {
             if (k >= 0) {  // a medium union: sorted now, kept in mtmp until level_write
                 uint32_t v;
                 warp_medium_sort(med[w], k, lane, v);
-                // the warp takes buffer space in slabs of kMedSlab elements (one atomic per slab,
-                // not one per union on a counter every warp of the level shares)
-                if (static_cast<unsigned long long>(k) > slab_left) {
-                    unsigned long long b = 0;
-                    if (lane == 0) b = atomicAdd(&st.info[4], static_cast<unsigned long long>(kMedSlab));
-                    slab_base = __shfl_sync(0xFFFFFFFFu, b, 0);
-                    slab_left = slab_base + kMedSlab <= st.mtmp_cap ? kMedSlab : 0;
-                }
-                const unsigned long long at = slab_base;
-                if (static_cast<unsigned long long>(k) <= slab_left) {
-                    slab_base += k;
-                    slab_left -= k;
+                const unsigned long long at = take(static_cast<unsigned long long>(k));
+                if (at != ~0ull) {
                     if (k <= 32) {
                         if (static_cast<int>(lane) < k) st.mtmp[at + lane] = v;
                     } else {
@@ -1240,6 +1252,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         gather_u32<<<grid_for(ctx, nb), 256, 0, s>>>(edt2, balls, nb, ball_r2);
         ctx->check_launch("gather_u32");
     }
+    auto kt_balls_host = std::make_unique<KernelTimer>(ctx, "pores_balls_to_host");
     std::vector<uint32_t> h_idx(nb), h_r2(nb);
     if (nb) {
         PMA_CUDA(cudaMemcpyAsync(h_idx.data(), balls, nb * 4, cudaMemcpyDeviceToHost, s));
@@ -1254,6 +1267,8 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     std::vector<unsigned long long> items(nb);
     for (int64_t i = 0; i < nb; ++i)
         items[i] = (static_cast<unsigned long long>(h_r2[i]) << 32) | static_cast<unsigned long long>(i);
+    std::vector<uint32_t> voxel_of_rank(nb);  // declared before the joiner: outlives the thread
+    kt_balls_host.reset();
     struct Joiner {
         std::thread t;
         ~Joiner() {
@@ -1264,10 +1279,26 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     // of the time, the top partition steps run on one to eight threads
     int sort_levels = 1;
     while (sort_levels < 4 && (2u << sort_levels) <= std::thread::hardware_concurrency()) ++sort_levels;
-    sorter.t = std::thread([&items, sort_levels] {
+    // then the voxel of each rank, gathered on host threads too (a random read per ball)
+    sorter.t = std::thread([&items, &h_idx, &voxel_of_rank, sort_levels] {
         ordered_sort(
             items.begin(), items.end(),
             [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); }, sort_levels);
+        const int64_t m = static_cast<int64_t>(items.size());
+        auto gather = [&](int64_t lo, int64_t hi) {
+            for (int64_t r = lo; r < hi; ++r) voxel_of_rank[r] = h_idx[items[r] & 0xFFFFFFFFull];
+        };
+        const int nt = m >= (1 << 20) ? (1 << sort_levels) : 1;
+        std::vector<std::thread> ts;
+        for (int t = 1; t < nt; ++t) {
+            try {
+                ts.emplace_back(gather, m * t / nt, m * (t + 1) / nt);
+            } catch (const std::system_error&) {
+                gather(m * t / nt, m * (t + 1) / nt);  // no thread to be had: in line
+            }
+        }
+        gather(0, m / nt);
+        for (auto& th : ts) th.join();
     });
 
     // Plateaus: connected sets of equal crad under the stencil.
@@ -1384,8 +1415,6 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     sorter.t.join();
     kt_join.reset();
     auto kt_stats = std::make_unique<KernelTimer>(ctx, "plateau_stats");
-    std::vector<uint32_t> voxel_of_rank(nb);
-    for (int64_t r = 0; r < nb; ++r) voxel_of_rank[r] = h_idx[items[r] & 0xFFFFFFFFull];
     uint32_t* crank = buf<uint32_t>(ctx, "pores.crank", n);
     fill_u32<<<G, 256, 0, s>>>(crank, n, kNone);
     ctx->check_launch("fill_u32");
@@ -1476,7 +1505,11 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             PMA_CUDA(cudaMemsetAsync(ps.info, 0, 40, s));
             {
                 KernelTimer kt2(ctx, "level_seeds");
-                level_seeds<<<lg, kLevelWarps * 32, 0, s>>>(ps, b, e);
+                // slabs small enough for every warp of the launch to get some of mtmp, and
+                // at least a medium union's largest size
+                const unsigned slab = static_cast<unsigned>(std::min<unsigned long long>(
+                    kMedSlab, std::max<unsigned long long>(kMedCap, ps.mtmp_cap / (1ull * lg * kLevelWarps))));
+                level_seeds<<<lg, kLevelWarps * 32, 0, s>>>(ps, b, e, slab);
                 level_heavy<<<heavy_grid, 512, 0, s>>>(ps, b);
                 ctx->count_launch(2);
             }
