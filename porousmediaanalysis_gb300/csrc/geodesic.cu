@@ -55,7 +55,7 @@ struct Geo {
 struct Frontier {
     uint32_t* bits;        // four bitmaps of nwords words: bucket b uses bitmap b & 3
     size_t nwords;
-    unsigned int* count;   // [4] voxels set in each bitmap
+    unsigned int* count;   // [4] non-zero when a voxel was marked in that bitmap
     uint32_t* list;        // the compacted bucket being swept
     unsigned int* list_n;  // its length
     uint32_t cap;          // list capacity
@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
 // order, so a warp's loads of one stencil position fall on neighbouring addresses), then
 // lowers the neighbours it improves. Each voxel is in the list once, so a live entry
 // (bucket(dist) == k) is settled exactly once. Steps are in [1, 2), so pushes go to buckets
-// k + 1 and k + 2 only; they are counted per thread and added per warp at the end.
+// k + 1 and k + 2 only; whether a bucket got any is flagged per warp at the end (the host
+// only asks whether the next buckets are empty).
 // Four blocks per SM (64 registers; the float64 form spills about 100 bytes to L1): more
 // warps hide more of the neighbour loads' latency than the spilled registers cost (the float64
 // bucket loop of the 1024^3 spinodal: 338 ms at 120 registers, 299 ms at three blocks per SM,
@@ -187,18 +188,23 @@ __global__ void __launch_bounds__(256, 4) geo_bucket(Geo g, T w1, T w2, T w3, T*
             if (kk == 0 || (D3Q7 && kk != 1)) continue;
             const T nd = kk == 1 ? nd1 : (kk == 2 ? nd2 : nd3);
             if (nd < nb[j]) {
+                // Neither update waits for its old value (reductions, no round trip): the bit
+                // marks the voxel in nd's bucket even when another thread has lowered it further
+                // meanwhile, and such an entry is skipped as stale when its bucket comes (the
+                // lowest value's bucket has its bit from the thread that wrote that value).
                 const size_t w = static_cast<size_t>(static_cast<long long>(v) + dz * sxy + dx * sy + dy);
-                const U old = atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
-                if (Bits<T>::to(nd) < old) {
-                    const int pb = Bits<T>::bucket(nd);
-                    const uint32_t bit = 1u << (w & 31);
-                    if (pb == k + 1) {
-                        c1 += (atomicOr(&bm1[w >> 5], bit) & bit) ? 0u : 1u;
-                    } else if (pb == k + 2) {
-                        c2 += (atomicOr(&bm2[w >> 5], bit) & bit) ? 0u : 1u;
-                    } else if (!(atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit) & bit)) {
-                        atomicAdd(&f.count[pb & 3], 1u);  // not reachable with steps in [1, 2)
-                    }
+                atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
+                const int pb = Bits<T>::bucket(nd);
+                const uint32_t bit = 1u << (w & 31);
+                if (pb == k + 1) {
+                    atomicOr(&bm1[w >> 5], bit);
+                    c1 = 1;
+                } else if (pb == k + 2) {
+                    atomicOr(&bm2[w >> 5], bit);
+                    c2 = 1;
+                } else {  // not reachable with steps in [1, 2)
+                    atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit);
+                    atomicOr(&f.count[pb & 3], 1u);
                 }
             }
         }
@@ -206,14 +212,14 @@ __global__ void __launch_bounds__(256, 4) geo_bucket(Geo g, T w1, T w2, T w3, T*
     for (int o = 16; o > 0; o >>= 1) {
         my_settled += __shfl_xor_sync(0xFFFFFFFFu, my_settled, o);
         my_walls |= __shfl_xor_sync(0xFFFFFFFFu, my_walls, o);
-        c1 += __shfl_xor_sync(0xFFFFFFFFu, c1, o);
-        c2 += __shfl_xor_sync(0xFFFFFFFFu, c2, o);
+        c1 |= __shfl_xor_sync(0xFFFFFFFFu, c1, o);
+        c2 |= __shfl_xor_sync(0xFFFFFFFFu, c2, o);
     }
     if ((threadIdx.x & 31) == 0) {
         if (my_settled) atomicAdd(f.settled, my_settled);
         if (my_walls) atomicOr(f.walls, my_walls);
-        if (c1) atomicAdd(&f.count[(k + 1) & 3], c1);
-        if (c2) atomicAdd(&f.count[(k + 2) & 3], c2);
+        if (c1) atomicOr(&f.count[(k + 1) & 3], 1u);
+        if (c2) atomicOr(&f.count[(k + 2) & 3], 1u);
     }
 }
 

@@ -601,14 +601,30 @@ __device__ __forceinline__ int warp_medium_insert(const PlateauSets& st, unsigne
         }
         over = true;  // table full (only after more than kMedCap insertions)
     };
-    for (unsigned e = e0 + lane; e < e1 && !over; e += 32) {
-        const uint32_t q = __ldg(st.edges + e);
-        const uint32_t len = __ldg(st.slen + q);
-        const uint32_t* src = st.pool + __ldg(st.soff + q);
-        for (uint32_t k = 0; k < len && !over; ++k) {
-            insert(__ldg(src + k));
-            // another lane may have passed the cap: stop early
-            if (*reinterpret_cast<volatile unsigned int*>(&mb.count) > static_cast<unsigned>(kMedCap)) over = true;
+    // The warp streams through the predecessors' sets one set at a time, 32 elements a step
+    // (lanes take 32 edges' sizes and offsets at once, then broadcast them): a set of
+    // thousands of elements costs its length / 32 steps, not its length on one lane.
+    bool stop = false;
+    for (unsigned eb = e0; eb < e1 && !stop; eb += 32) {
+        uint32_t len = 0;
+        unsigned long long off = 0;
+        if (eb + lane < e1) {
+            const uint32_t q = __ldg(st.edges + eb + lane);
+            len = __ldg(st.slen + q);
+            off = __ldg(st.soff + q);
+        }
+        const unsigned ne = min(32u, e1 - eb);
+        for (unsigned t = 0; t < ne && !stop; ++t) {
+            const uint32_t tl = __shfl_sync(0xFFFFFFFFu, len, t);
+            const uint32_t* src = st.pool + __shfl_sync(0xFFFFFFFFu, off, t);
+            for (uint32_t b = 0; b < tl; b += 32) {  // warp-uniform steps
+                if (b + lane < tl) insert(__ldg(src + b + lane));
+                // past the cap on any lane: the union takes the sort path
+                if (__any_sync(0xFFFFFFFFu, over)) {
+                    stop = true;
+                    break;
+                }
+            }
         }
     }
     if (seed != kNone && lane == 0 && !over) insert(seed);
@@ -952,13 +968,26 @@ __global__ void __launch_bounds__(1024) level_merge_small(PlateauSets st, size_t
         const uint32_t p = st.order[begin + L];
         const unsigned e0 = st.eoff[p], e1 = st.eoff[p + 1];
         const unsigned long long hi = static_cast<unsigned long long>(b) << 32;
-        for (unsigned e = e0 + lane; e < e1; e += 32) {
-            const uint32_t q = __ldg(st.edges + e);
-            const uint32_t len = __ldg(st.slen + q);
-            const uint32_t* src = st.pool + __ldg(st.soff + q);
-            const unsigned pos = atomicAdd(&s_count, len);
-            for (uint32_t k = 0; k < len; ++k)
-                if (pos + k < kSmallMerge) sk[pos + k] = hi | __ldg(src + k);
+        // lanes take 32 edges' sets at once and reserve their room; the warp then copies the
+        // sets one after another, 32 elements a step
+        for (unsigned eb = e0; eb < e1; eb += 32) {
+            uint32_t len = 0;
+            unsigned long long off = 0;
+            unsigned pos = 0;
+            if (eb + lane < e1) {
+                const uint32_t q = __ldg(st.edges + eb + lane);
+                len = __ldg(st.slen + q);
+                off = __ldg(st.soff + q);
+                pos = atomicAdd(&s_count, len);
+            }
+            const unsigned ne = min(32u, e1 - eb);
+            for (unsigned t = 0; t < ne; ++t) {
+                const uint32_t tl = __shfl_sync(0xFFFFFFFFu, len, t);
+                const unsigned tp = __shfl_sync(0xFFFFFFFFu, pos, t);
+                const uint32_t* src = st.pool + __shfl_sync(0xFFFFFFFFu, off, t);
+                for (uint32_t r = lane; r < tl; r += 32)
+                    if (tp + r < kSmallMerge) sk[tp + r] = hi | __ldg(src + r);
+            }
         }
         if (lane == 0 && st.seed[p] != kNone) {
             const unsigned pos = atomicAdd(&s_count, 1u);
@@ -1275,10 +1304,14 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             if (t.joinable()) t.join();
         }
     } sorter;
-    // up to 16 leaf tasks (levels 4) where the host has the cores: the leaves' sorts are most
-    // of the time, the top partition steps run on one to eight threads
-    int sort_levels = 1;
-    while (sort_levels < 4 && (2u << sort_levels) <= std::thread::hardware_concurrency()) ++sort_levels;
+    // up to 16 leaf tasks (levels 4) where the host has the cores and each leaf gets at least
+    // 2^16 balls: the leaves' sorts are most of the time, the top partition steps run on one
+    // to eight threads; small volumes (the batched and serving forms run many at once) sort
+    // on this one thread
+    int sort_levels = 0;
+    while (sort_levels < 4 && (2u << sort_levels) <= std::thread::hardware_concurrency() &&
+           (static_cast<unsigned long long>(nb) >> (16 + sort_levels + 1)) > 0)
+        ++sort_levels;
     // then the voxel of each rank, gathered on host threads too (a random read per ball)
     sorter.t = std::thread([&items, &h_idx, &voxel_of_rank, sort_levels] {
         ordered_sort(
@@ -1501,6 +1534,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
             int lclass = 0;
             while (lclass < 31 && (2ull << lclass) <= e - b) ++lclass;
             KernelTimer kt_level(ctx, kLevelClass[lclass]);
+            if (ctx->timing) ctx->count(std::string(kLevelClass[lclass]) + ".count", 1);
             const unsigned lg = grid_for(ctx, (e - b) * 32, kLevelWarps * 32);
             PMA_CUDA(cudaMemsetAsync(ps.info, 0, 40, s));
             {
