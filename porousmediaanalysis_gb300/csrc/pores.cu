@@ -1147,6 +1147,9 @@ __global__ void group_starts(const uint32_t* __restrict__ sorted_p, const unsign
                              unsigned int* __restrict__ err) {
     PMA_GRID_STRIDE(i, nm) {
         bool s = (i == 0) || h1[i] != h1[i - 1] || h2[i] != h2[i - 1];
+        // equal first hashes, different second ones: sorted by the first hash alone, such sets
+        // may interleave (the host then sorts by both)
+        if (i > 0 && h1[i] == h1[i - 1] && h2[i] != h2[i - 1]) atomicOr(err, 64u);
         if (!s) {
             const uint32_t a = sorted_p[i], b = sorted_p[i - 1];
             bool eq = slen[a] == slen[b];
@@ -1228,9 +1231,10 @@ __global__ void voxel_labels(const uint32_t* __restrict__ pid, const uint32_t* _
 // Old -> new label remap by binary search in sorted old ids.
 __global__ void remap_labels(uint32_t* __restrict__ labels, size_t n, const uint32_t* __restrict__ old_ids,
                              const uint32_t* __restrict__ new_ids, uint32_t m) {
+    const uint32_t first = m ? old_ids[0] : 0xFFFFFFFFu;  // pore labels are below every type id
     PMA_GRID_STRIDE(v, n) {
         const uint32_t l = labels[v];
-        if (l == 0) continue;
+        if (l == 0 || l < first || m == 0) continue;
         uint32_t lo = 0, hi = m;
         while (lo < hi) {
             const uint32_t mid = (lo + hi) >> 1;
@@ -1747,20 +1751,37 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         auto* ktmp = buf<unsigned long long>(ctx, "pores.ktmp", nm);
         uint32_t* v1 = buf<uint32_t>(ctx, "pores.v1", nm);
         uint32_t* v2 = buf<uint32_t>(ctx, "pores.v2", nm);
-        // Group plateaus with equal seed sets: stable radix sorts by h2 then by h1, so equal
-        // (h1, h2) pairs end up adjacent.
-        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, multi, nm, h1, h2);
-        ctx->check_launch("throat_hashes");
-        sort_pairs(ctx, h2, ktmp, multi, v1, nm);
-        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v1, nm, h1, h2);
-        ctx->check_launch("throat_hashes");
-        sort_pairs(ctx, h1, ktmp, v1, v2, nm);
-        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v2, nm, h1, h2);
-        ctx->check_launch("throat_hashes");
+        // Group plateaus with equal seed sets: a radix sort by the first hash puts equal sets
+        // side by side unless two different sets share it (about n^2 / 2^65 likely), which
+        // group_starts flags; then stable sorts by the second hash and then the first put
+        // equal (h1, h2) pairs side by side.
         uint32_t* gstart = buf<uint32_t>(ctx, "pores.gstart", nm);
         uint32_t* gid = buf<uint32_t>(ctx, "pores.gid", nm);
+        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, multi, nm, h1, h2);
+        ctx->check_launch("throat_hashes");
+        sort_pairs(ctx, h1, ktmp, multi, v2, nm);
+        throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v2, nm, h1, h2);
+        ctx->check_launch("throat_hashes");
         group_starts<<<grid_for(ctx, nm), 256, 0, s>>>(v2, h1, h2, nm, ps.soff, ps.slen, ps.pool, gstart, err);
         ctx->check_launch("group_starts");
+        {
+            unsigned int h_err0 = 0;
+            PMA_CUDA(cudaMemcpyAsync(&h_err0, err, 4, cudaMemcpyDeviceToHost, s));
+            ctx->sync();
+            if (h_err0 & 64u) {
+                PMA_CUDA(cudaMemsetAsync(err, 0, 4, s));
+                throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, multi, nm, h1, h2);
+                ctx->check_launch("throat_hashes");
+                sort_pairs(ctx, h2, ktmp, multi, v1, nm);
+                throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v1, nm, h1, h2);
+                ctx->check_launch("throat_hashes");
+                sort_pairs(ctx, h1, ktmp, v1, v2, nm);
+                throat_hashes<<<grid_for(ctx, nm), 256, 0, s>>>(ps.soff, ps.slen, ps.pool, v2, nm, h1, h2);
+                ctx->check_launch("throat_hashes");
+                group_starts<<<grid_for(ctx, nm), 256, 0, s>>>(v2, h1, h2, nm, ps.soff, ps.slen, ps.pool, gstart, err);
+                ctx->check_launch("group_starts");
+            }
+        }
         exclusive_sum(ctx, gstart, gid, nm);
         uint32_t last_off = 0, last_start = 0;
         PMA_CUDA(cudaMemcpyAsync(&last_off, gid + nm - 1, 4, cudaMemcpyDeviceToHost, s));
@@ -1945,6 +1966,7 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
     KernelTimer kt_stage(ctx, "stage_removal");
     check_dims(d);
     PMA_REQUIRE(labels, PMA_ERR_ARGUMENT, "pma_remove_empty_pores: null labels");
+    auto kt_host = std::make_unique<KernelTimer>(ctx, "removal_tables");
     // EPR.cpp:193-244: drop zero-volume pores and remove them from the type lists.
     std::vector<uint32_t> empty;
     std::vector<pma_pore> kept;
@@ -2024,6 +2046,7 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
     t->throats.swap(throats);
     t->pool.swap(pool);
     std::sort(remap.begin(), remap.end());
+    kt_host.reset();
     if (remap.empty()) return;  // EPR.cpp:54-57
     std::vector<uint32_t> o, nw;
     for (auto& kv : remap) {
