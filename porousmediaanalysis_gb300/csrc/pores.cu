@@ -31,6 +31,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <chrono>
 #include <thread>
 #include <vector>
 
@@ -66,6 +67,11 @@ __global__ void scatter_seed_ids(const uint32_t* __restrict__ up, size_t npores,
         rank2pore[up[k]] = static_cast<uint32_t>(k);
         rank2id[up[k]] = up[npores + k];
     }
+}
+
+__global__ void pack_items(const uint32_t* __restrict__ r2, const uint32_t* __restrict__ idx, size_t n,
+                           unsigned long long* __restrict__ items) {
+    PMA_GRID_STRIDE(i, n) items[i] = (static_cast<unsigned long long>(r2[i]) << 32) | idx[i];
 }
 
 __global__ void scatter_rank(const uint32_t* __restrict__ voxel_of_rank, size_t n,
@@ -1297,22 +1303,22 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
         gather_u32<<<grid_for(ctx, nb), 256, 0, s>>>(edt2, balls, nb, ball_r2);
         ctx->check_launch("gather_u32");
     }
-    auto kt_balls_host = std::make_unique<KernelTimer>(ctx, "pores_balls_to_host");
-    std::vector<uint32_t> h_idx(nb), h_r2(nb);
-    if (nb) {
-        PMA_CUDA(cudaMemcpyAsync(h_idx.data(), balls, nb * 4, cudaMemcpyDeviceToHost, s));
-        PMA_CUDA(cudaMemcpyAsync(h_r2.data(), ball_r2, nb * 4, cudaMemcpyDeviceToHost, s));
-        ctx->sync();
-    }
     // std::sort with the reference's comparator (PoreAndThroatComputer.cpp:121-122), run on
     // host threads (ordered_sort: the same permutation) while the plateau kernels below run.
-    // The items are 8-byte (r2, scan index) pairs compared on r2 alone: std::sort's moves
+    // The items are 8-byte (r2, voxel index) pairs compared on r2 alone: std::sort's moves
     // depend only on comparison results, so the permutation equals the one the reference's
-    // 16-byte balls go through.
-    std::vector<unsigned long long> items(nb);
-    for (int64_t i = 0; i < nb; ++i)
-        items[i] = (static_cast<unsigned long long>(h_r2[i]) << 32) | static_cast<unsigned long long>(i);
-    std::vector<uint32_t> voxel_of_rank(nb);  // declared before the joiner: outlives the thread
+    // 16-byte balls go through, and the sorted items carry each rank's voxel. They are packed
+    // on the device and sorted in a page-locked buffer of the context.
+    auto kt_balls_host = std::make_unique<KernelTimer>(ctx, "pores_balls_to_host");
+    auto* items = static_cast<unsigned long long*>(ctx->host_buffer("pores.items", nb * 8));
+    auto* voxel_of_rank = static_cast<uint32_t*>(ctx->host_buffer("pores.voxel_of_rank", nb * 4));
+    if (nb) {
+        auto* d_items = buf<unsigned long long>(ctx, "pores.d_items", nb);
+        pack_items<<<grid_for(ctx, nb), 256, 0, s>>>(ball_r2, balls, nb, d_items);
+        ctx->check_launch("pack_items");
+        copy_to_host(ctx, items, d_items, nb * 8);
+        ctx->sync();
+    }
     kt_balls_host.reset();
     struct Joiner {
         std::thread t;
@@ -1328,14 +1334,14 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     while (sort_levels < 4 && (2u << sort_levels) <= std::thread::hardware_concurrency() &&
            (static_cast<unsigned long long>(nb) >> (16 + sort_levels + 1)) > 0)
         ++sort_levels;
-    // then the voxel of each rank, gathered on host threads too (a random read per ball)
-    sorter.t = std::thread([&items, &h_idx, &voxel_of_rank, sort_levels] {
+    // then the voxel of each rank, taken from the sorted items on host threads too
+    sorter.t = std::thread([items, voxel_of_rank, nb, sort_levels] {
         ordered_sort(
-            items.begin(), items.end(),
+            items, items + nb,
             [](unsigned long long a, unsigned long long b) { return (a >> 32) > (b >> 32); }, sort_levels);
-        const int64_t m = static_cast<int64_t>(items.size());
+        const int64_t m = nb;
         auto gather = [&](int64_t lo, int64_t hi) {
-            for (int64_t r = lo; r < hi; ++r) voxel_of_rank[r] = h_idx[items[r] & 0xFFFFFFFFull];
+            for (int64_t r = lo; r < hi; ++r) voxel_of_rank[r] = static_cast<uint32_t>(items[r]);
         };
         const int nt = m >= (1 << 20) ? (1 << sort_levels) : 1;
         std::vector<std::thread> ts;
@@ -1469,7 +1475,7 @@ pma_table* pores(pma_ctx* ctx, const uint8_t* mask, const uint32_t* edt2, const 
     fill_u32<<<G, 256, 0, s>>>(crank, n, kNone);
     ctx->check_launch("fill_u32");
     if (nb) {
-        PMA_CUDA(cudaMemcpyAsync(balls, voxel_of_rank.data(), nb * 4, cudaMemcpyHostToDevice, s));
+        copy_from_host(ctx, balls, voxel_of_rank, nb * 4);
         scatter_rank<<<grid_for(ctx, nb), 256, 0, s>>>(balls, nb, crank);
         ctx->check_launch("scatter_rank");
     }
@@ -1967,6 +1973,12 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
     check_dims(d);
     PMA_REQUIRE(labels, PMA_ERR_ARGUMENT, "pma_remove_empty_pores: null labels");
     auto kt_host = std::make_unique<KernelTimer>(ctx, "removal_tables");
+    auto mark = std::chrono::steady_clock::now();
+    auto phase = [&](const char* name) {  // host time of each part, with the timing report
+        const auto now = std::chrono::steady_clock::now();
+        ctx->count(name, std::chrono::duration<double, std::milli>(now - mark).count());
+        mark = now;
+    };
     // EPR.cpp:193-244: drop zero-volume pores and remove them from the type lists.
     std::vector<uint32_t> empty;
     std::vector<pma_pore> kept;
@@ -1993,6 +2005,8 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
         loff[k + 1] = lists.size();
     }
     auto len = [&](size_t k) { return loff[k + 1] - loff[k]; };
+    phase("removal.filter_ms");
+    ctx->count("removal.types", static_cast<double>(nt));
     std::vector<char> alive(nt, 1);
     std::vector<std::pair<uint32_t, uint32_t>> remap;  // (old id, new id)
     // EPR.cpp:167-191: types with fewer than two pores.
@@ -2001,35 +2015,45 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
             if (len(k) == 1) remap.emplace_back(t->throats[by_id[k]].id, lists[loff[k]]);
             alive[k] = 0;
         }
-    // EPR.cpp:126-165: merge types with equal pore lists into the largest id.
-    std::vector<uint32_t> live;
-    for (size_t k = 0; k < nt; ++k)
-        if (alive[k]) live.push_back(static_cast<uint32_t>(k));
-    auto less_list = [&](uint32_t a, uint32_t b) {
-        return std::lexicographical_compare(lists.begin() + loff[a], lists.begin() + loff[a + 1],
-                                            lists.begin() + loff[b], lists.begin() + loff[b + 1]);
-    };
+    // EPR.cpp:126-165: merge types with equal pore lists into the largest id. Lists are put
+    // side by side through a hash of their contents and grouped by comparing them element by
+    // element within a hash (the groups, not their order, decide the result).
     auto same_list = [&](uint32_t a, uint32_t b) {
         return len(a) == len(b) && std::equal(lists.begin() + loff[a], lists.begin() + loff[a + 1],
                                               lists.begin() + loff[b]);
     };
-    std::stable_sort(live.begin(), live.end(), less_list);
+    std::vector<std::pair<unsigned long long, uint32_t>> live;  // (hash of the list, type)
+    for (size_t k = 0; k < nt; ++k) {
+        if (!alive[k]) continue;
+        unsigned long long h = 1469598103934665603ull ^ len(k);
+        for (size_t i = loff[k]; i < loff[k + 1]; ++i) h = (h ^ lists[i]) * 1099511628211ull;
+        live.emplace_back(h, static_cast<uint32_t>(k));
+    }
+    std::sort(live.begin(), live.end());
+    std::vector<uint32_t> members;
     for (size_t i = 0; i < live.size();) {
         size_t j = i + 1;
-        while (j < live.size() && same_list(live[i], live[j])) ++j;
-        if (j - i > 1) {
+        while (j < live.size() && live[j].first == live[i].first) ++j;
+        for (size_t a = i; a < j && j - i > 1; ++a) {  // equal hashes: exact groups among them
+            if (!alive[live[a].second]) continue;
+            members.assign(1, live[a].second);
+            for (size_t b = a + 1; b < j; ++b)
+                if (alive[live[b].second] && same_list(live[a].second, live[b].second))
+                    members.push_back(live[b].second);
+            if (members.size() < 2) continue;
             uint32_t keep = 0;
-            for (size_t q = i; q < j; ++q) keep = std::max(keep, t->throats[by_id[live[q]]].id);
-            for (size_t q = i; q < j; ++q) {
-                const uint32_t id = t->throats[by_id[live[q]]].id;
+            for (uint32_t m : members) keep = std::max(keep, t->throats[by_id[m]].id);
+            for (uint32_t m : members) {
+                const uint32_t id = t->throats[by_id[m]].id;
                 if (id != keep) {
-                    alive[live[q]] = 0;
+                    alive[m] = 0;
                     remap.emplace_back(id, keep);
                 }
             }
         }
         i = j;
     }
+    phase("removal.merge_ms");
     std::vector<pma_throat> throats;
     std::vector<uint32_t> pool;
     for (size_t k = 0; k < nt; ++k) {
@@ -2046,6 +2070,7 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
     t->throats.swap(throats);
     t->pool.swap(pool);
     std::sort(remap.begin(), remap.end());
+    phase("removal.rows_ms");
     kt_host.reset();
     if (remap.empty()) return;  // EPR.cpp:54-57
     std::vector<uint32_t> o, nw;
