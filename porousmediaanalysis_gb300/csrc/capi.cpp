@@ -80,6 +80,26 @@ void* pma_ctx::host_staging(size_t bytes) {
     return pinned;
 }
 
+void* pma_ctx::host_buffer(const std::string& tag, size_t bytes) {
+    Buf& b = host_cache[tag];
+    if (b.ptr && b.bytes >= bytes) return b.ptr;
+    if (b.ptr) {
+        PMA_CUDA(cudaFreeHost(b.ptr));
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    const size_t want = std::max<size_t>(bytes + bytes / 8, 4096);
+    PMA_CUDA(cudaMallocHost(&b.ptr, want));
+    b.bytes = want;
+    return b.ptr;
+}
+
+void pma_ctx::free_host_buffers() {
+    for (auto& kv : host_cache)
+        if (kv.second.ptr) cudaFreeHost(kv.second.ptr);
+    host_cache.clear();
+}
+
 int64_t* pma_ctx::pinned_count() {
     if (!count_word) {
         void* p = nullptr;
@@ -154,6 +174,7 @@ int pma_ctx_destroy(pma_ctx* ctx) {
         if (ctx->sync_event) cudaEventDestroy(ctx->sync_event);
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
         if (ctx->count_word) cudaFreeHost(ctx->count_word);
+        ctx->free_host_buffers();
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
     });
@@ -285,6 +306,7 @@ int pma_ctx_trim(pma_ctx* ctx) {
         ctx->cache.clear();
         PMA_CUDA(cudaStreamSynchronize(ctx->stream));
         if (ctx->pool) PMA_CUDA(cudaMemPoolTrimTo(ctx->pool, 0));
+        ctx->free_host_buffers();
     });
 }
 

@@ -52,9 +52,15 @@ struct Geo {
     }
 };
 
+// Compaction chunks: 256 bitmap words (8192 voxels), one block step of geo_compact.
+constexpr int kChunkWords = 256;
+constexpr int kChunkShift = 13;  // voxel index -> chunk
+
 struct Frontier {
     uint32_t* bits;        // four bitmaps of nwords words: bucket b uses bitmap b & 3
     size_t nwords;
+    uint8_t* dirty;        // four flag arrays of nchunks bytes: a bit was set in the chunk
+    size_t nchunks;
     unsigned int* count;   // [4] non-zero when a voxel was marked in that bitmap
     uint32_t* list;        // the compacted bucket being swept
     unsigned int* list_n;  // its length
@@ -79,18 +85,22 @@ template <class T>
 __global__ void geo_start(Frontier f, T* dist, uint32_t v) {
     dist[v] = static_cast<T>(0);
     f.bits[v >> 5] |= 1u << (v & 31);  // bucket 0
+    f.dirty[v >> kChunkShift] = 1;
     f.count[0] = 1;
 }
 
 // Bucket k's bitmap -> list (voxel order within each block's 8192 voxels), cleared behind.
-__global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
-    __shared__ unsigned int wsum[8];
+// Only chunks whose flag is set are read: a bucket is a thin shell of the volume, and reading
+// the whole bitmap for each bucket took a quarter of the geodesic kernels' time at 512^3.
+__global__ void __launch_bounds__(kChunkWords) geo_compact(Frontier f, int k) {
+    __shared__ unsigned int wsum[kChunkWords / 32];
     __shared__ unsigned int base;
     uint32_t* bm = f.bits + static_cast<size_t>(k & 3) * f.nwords;
+    uint8_t* dirty = f.dirty + static_cast<size_t>(k & 3) * f.nchunks;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (size_t w0 = static_cast<size_t>(blockIdx.x) * blockDim.x; w0 < f.nwords;
-         w0 += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const size_t w = w0 + threadIdx.x;
+    for (size_t ch = blockIdx.x; ch < f.nchunks; ch += gridDim.x) {
+        if (!dirty[ch]) continue;  // the same byte for the whole block: a uniform skip
+        const size_t w = ch * kChunkWords + threadIdx.x;
         uint32_t word = 0;
         if (w < f.nwords) {
             word = bm[w];
@@ -103,10 +113,11 @@ __global__ void __launch_bounds__(256) geo_compact(Frontier f, int k) {
             if (lane >= static_cast<unsigned>(o)) incl += t;
         }
         if (lane == 31) wsum[warp] = incl;
-        __syncthreads();
+        __syncthreads();  // every thread has read the flag
         if (threadIdx.x == 0) {
+            dirty[ch] = 0;
             unsigned tot = 0;
-            for (int i = 0; i < 8; ++i) {
+            for (int i = 0; i < kChunkWords / 32; ++i) {
                 const unsigned v = wsum[i];
                 wsum[i] = tot;
                 tot += v;
@@ -148,8 +159,6 @@ __global__ void __launch_bounds__(256, 4) geo_bucket(Geo g, T w1, T w2, T w3, T*
     const long long sy = g.SY, sxy = static_cast<long long>(g.SX) * g.SY;
     unsigned long long my_settled = 0;
     unsigned my_walls = 0, c1 = 0, c2 = 0;
-    uint32_t* bm1 = f.bits + static_cast<size_t>((k + 1) & 3) * f.nwords;
-    uint32_t* bm2 = f.bits + static_cast<size_t>((k + 2) & 3) * f.nwords;
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t v = list[i];
         const T dv = dist[v];
@@ -196,16 +205,11 @@ __global__ void __launch_bounds__(256, 4) geo_bucket(Geo g, T w1, T w2, T w3, T*
                 atomicMin(reinterpret_cast<U*>(dist + w), Bits<T>::to(nd));
                 const int pb = Bits<T>::bucket(nd);
                 const uint32_t bit = 1u << (w & 31);
-                if (pb == k + 1) {
-                    atomicOr(&bm1[w >> 5], bit);
-                    c1 = 1;
-                } else if (pb == k + 2) {
-                    atomicOr(&bm2[w >> 5], bit);
-                    c2 = 1;
-                } else {  // not reachable with steps in [1, 2)
-                    atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit);
-                    atomicOr(&f.count[pb & 3], 1u);
-                }
+                atomicOr(&f.bits[static_cast<size_t>(pb & 3) * f.nwords + (w >> 5)], bit);
+                f.dirty[static_cast<size_t>(pb & 3) * f.nchunks + (w >> kChunkShift)] = 1;
+                if (pb == k + 1) c1 = 1;
+                else if (pb == k + 2) c2 = 1;
+                else atomicOr(&f.count[pb & 3], 1u);  // not reachable with steps in [1, 2)
             }
         }
     }
@@ -285,11 +289,15 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
     const uint32_t cap = static_cast<uint32_t>(std::min<size_t>(n, size_t(1) << 28));
     const size_t nwords = (n + 31) / 32;
     auto* bits = static_cast<uint32_t*>(ctx->scratch("geo.bits", 4 * nwords * 4));
+    const size_t nchunks = (nwords + kChunkWords - 1) / kChunkWords;
+    auto* dirty = static_cast<uint8_t*>(ctx->scratch("geo.dirty", 4 * nchunks));
     auto* list = static_cast<uint32_t*>(ctx->scratch("geo.list", static_cast<size_t>(cap) * 4));
     auto* misc = static_cast<unsigned long long*>(ctx->scratch("geo.misc", 64));
     Frontier f;
     f.bits = bits;
     f.nwords = nwords;
+    f.dirty = dirty;
+    f.nchunks = nchunks;
     f.list = list;
     f.count = reinterpret_cast<unsigned int*>(misc);          // 4 x u32 = misc[0..1]
     f.overflow = reinterpret_cast<unsigned int*>(misc + 2);   // misc[2] low
@@ -299,6 +307,7 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
     f.list_n = reinterpret_cast<unsigned int*>(misc + 6);     // misc[6] low
     f.cap = cap;
     PMA_CUDA(cudaMemsetAsync(bits, 0, 4 * nwords * 4, s));
+    PMA_CUDA(cudaMemsetAsync(dirty, 0, 4 * nchunks, s));
 
     geo_init<T><<<grid, 256, 0, s>>>(solid, n, dist, cavity);
     ctx->check_launch("geo_init");
@@ -319,7 +328,7 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
     const int max_buckets_per_sync = 32;
     const uint64_t bucket_limit = ctx->limits.geodesic_buckets ? ctx->limits.geodesic_buckets : 2ull * n + 64;
     const unsigned bucket_grid = static_cast<unsigned>(ctx->num_sms * 8);
-    const unsigned compact_grid = static_cast<unsigned>(std::min<size_t>(div_up(nwords, 256), ctx->num_sms * 8ull));
+    const unsigned compact_grid = static_cast<unsigned>(std::min<size_t>(nchunks, ctx->num_sms * 8ull));
     while (true) {  // SPC.cpp:94-140
         ++half;
         // SelectStartingPosition (SPC.cpp:396-426)
@@ -386,7 +395,7 @@ std::vector<pma_cavity> geodesic(pma_ctx* ctx, const uint8_t* solid, pma_dims d,
             KernelTimer kt(ctx, "geo_bucket");
             for (int i = 0; i < max_buckets_per_sync; ++i, ++k) {
                 geo_next<<<1, 1, 0, s>>>(f, k);
-                geo_compact<<<compact_grid, 256, 0, s>>>(f, k);
+                geo_compact<<<compact_grid, kChunkWords, 0, s>>>(f, k);
                 if (d3q7) geo_bucket<T, true><<<bucket_grid, 256, 0, s>>>(g, w1, w2, w3, dist, cavity, f, k, cavity_id);
                 else geo_bucket<T, false><<<bucket_grid, 256, 0, s>>>(g, w1, w2, w3, dist, cavity, f, k, cavity_id);
             }

@@ -111,6 +111,11 @@ struct pma_ctx {
     }
     void release(const std::string& tag);  // frees one scratch buffer (after the stream's work)
     void* host_staging(size_t bytes);
+    // Page-locked host buffers by name, grow-only until trimmed (host copies of large device
+    // arrays that the host works on, moved by the streaming copy kernel).
+    std::map<std::string, Buf> host_cache;
+    void* host_buffer(const std::string& tag, size_t bytes);
+    void free_host_buffers();
     int64_t* pinned_count();  // a pinned word of its own for counts read back after CUB calls
     int64_t* count_word = nullptr;
     void sync();

@@ -806,6 +806,9 @@ __global__ void ws_group_starts(const uint32_t* __restrict__ rec, size_t nr,
         if (!s) {
             const uint32_t q = rec[i - 1];
             s = rh1[r] != rh1[q] || rh2[r] != rh2[q];
+            // equal first hashes, different second ones: sorted by the first hash alone, such
+            // prefixes may interleave (the host then sorts by both)
+            if (rh1[r] == rh1[q] && rh2[r] != rh2[q]) atomicOr(err, 64u);
             if (!s) {  // verify: same prefix
                 const RecRef a = ws_rec(r, rvox, koff), b = ws_rec(q, rvox, koff);
                 bool eq = a.L == b.L;
@@ -1191,17 +1194,29 @@ pma_table* watershed(pma_ctx* ctx, const pma_table* pt, const uint32_t* crad2, p
     uint32_t* rec2 = buf<uint32_t>(ctx, "ws.rec2", nr);
     ws_iota<<<grid_for(ctx, nr), 256, 0, s>>>(rec, nr);
     ctx->check_launch("ws_iota");
-    // equal prefixes become adjacent: stable sorts by h2, then by h1 (values: record ids)
+    // Equal prefixes become adjacent: a radix sort by the first hash (values: record ids),
+    // unless two different prefixes share it (about n^2 / 2^65 likely), which ws_group_starts
+    // flags; then stable sorts by the second hash and then the first.
     auto* kh = buf<unsigned long long>(ctx, "ws.kh", nr);
     auto* kh2 = buf<unsigned long long>(ctx, "ws.kh2", nr);
-    sort_pairs(ctx, rh2, kh2, rec, rec2, nr);
-    ws_gather_h<<<grid_for(ctx, nr), 256, 0, s>>>(rh1, rec2, nr, kh);
-    ctx->check_launch("ws_gather_h");
-    sort_pairs(ctx, kh, kh2, rec2, rec, nr);
     uint32_t* gstart = buf<uint32_t>(ctx, "ws.gstart", nr);
     uint32_t* gexcl = buf<uint32_t>(ctx, "ws.gexcl", nr);
-    ws_group_starts<<<grid_for(ctx, nr), 256, 0, s>>>(rec, nr, rh1, rh2, kseq, koff, rvox, gstart, ws.err);
+    sort_pairs(ctx, rh1, kh2, rec, rec2, nr);
+    ws_group_starts<<<grid_for(ctx, nr), 256, 0, s>>>(rec2, nr, rh1, rh2, kseq, koff, rvox, gstart, ws.err);
     ctx->check_launch("ws_group_starts");
+    PMA_CUDA(cudaMemcpyAsync(&h_err, ws.err, 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    if (h_err & 64u) {
+        PMA_CUDA(cudaMemsetAsync(ws.err, 0, 4, s));
+        sort_pairs(ctx, rh2, kh2, rec, rec2, nr);
+        ws_gather_h<<<grid_for(ctx, nr), 256, 0, s>>>(rh1, rec2, nr, kh);
+        ctx->check_launch("ws_gather_h");
+        sort_pairs(ctx, kh, kh2, rec2, rec, nr);
+        PMA_CUDA(cudaMemcpyAsync(rec2, rec, nr * 4, cudaMemcpyDeviceToDevice, s));
+        ws_group_starts<<<grid_for(ctx, nr), 256, 0, s>>>(rec2, nr, rh1, rh2, kseq, koff, rvox, gstart, ws.err);
+        ctx->check_launch("ws_group_starts");
+    }
+    rec = rec2;  // records in group order from here on
     exclusive_sum(ctx, gstart, gexcl, nr);
     uint32_t last[2] = {0, 0};
     PMA_CUDA(cudaMemcpyAsync(&last[0], gexcl + nr - 1, 4, cudaMemcpyDeviceToHost, s));
