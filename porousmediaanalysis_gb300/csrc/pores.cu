@@ -1987,21 +1987,27 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
         else kept.push_back(p);
     }
     std::sort(empty.begin(), empty.end());
+    // empty pores by id (pore ids are below every type id and dense enough for a flag array)
+    uint32_t max_pore = 0;
+    for (const pma_pore& p : t->pores) max_pore = std::max(max_pore, p.id);
+    std::vector<uint8_t> is_empty(static_cast<size_t>(max_pore) + 1, 0);
+    for (uint32_t id : empty) is_empty[id] = 1;
     // Types in ascending id order with sorted, filtered pore lists (flat arrays).
     const size_t nt = t->throats.size();
     std::vector<uint32_t> by_id(nt);
     for (size_t i = 0; i < nt; ++i) by_id[i] = static_cast<uint32_t>(i);
-    std::sort(by_id.begin(), by_id.end(),
-              [&](uint32_t a, uint32_t b) { return t->throats[a].id < t->throats[b].id; });
+    auto id_less = [&](uint32_t a, uint32_t b) { return t->throats[a].id < t->throats[b].id; };
+    if (!std::is_sorted(by_id.begin(), by_id.end(), id_less)) std::sort(by_id.begin(), by_id.end(), id_less);
     std::vector<uint32_t> lists;
+    lists.reserve(t->pool.size());
     std::vector<size_t> loff(nt + 1, 0);
     std::vector<uint32_t> tmp;
     for (size_t k = 0; k < nt; ++k) {
         const pma_throat& th = t->throats[by_id[k]];
         tmp.assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
-        std::sort(tmp.begin(), tmp.end());
+        if (!std::is_sorted(tmp.begin(), tmp.end())) std::sort(tmp.begin(), tmp.end());
         for (uint32_t pid : tmp)
-            if (!std::binary_search(empty.begin(), empty.end(), pid)) lists.push_back(pid);
+            if (pid > max_pore || !is_empty[pid]) lists.push_back(pid);
         loff[k + 1] = lists.size();
     }
     auto len = [&](size_t k) { return loff[k + 1] - loff[k]; };
