@@ -587,8 +587,11 @@ __device__ __forceinline__ int warp_small_union(const PlateauSets& st, unsigned 
 // same seeds (a plateau's in-edges mostly come from plateaus reached by the same pores). One
 // warp inserts every element into a hash set of its own in shared memory; when at most kMedCap
 // distinct elements remain, they are sorted in the warp and the union stays on this path
-// instead of the expand-and-sort path of the big sets.
-constexpr unsigned kMedSum = 8192;
+// instead of the expand-and-sort path of the big sets. One warp streams a union's elements
+// serially, so a long one delays its whole level: at 1024^3 the sweep took 269 ms with unions of
+// up to 8192 elements here, 261 with 4096, 257 with 2048 (the rest going to the parallel sort
+// path).
+constexpr unsigned kMedSum = 2048;
 constexpr int kMedCap = 128;
 constexpr int kMedHash = 256;  // slots (power of two, twice kMedCap)
 constexpr unsigned long long kMedSlab = 1024;  // buffer space a warp takes at a time
