@@ -17,8 +17,12 @@ int main() {
         auto b = a;
         auto less = [](unsigned long long x, unsigned long long y) { return (x >> 32) > (y >> 32); };
         std::sort(a.begin(), a.end(), less);
+        auto c = b;
         pma::ordered_sort(b.begin(), b.end(), less, 1 + t % 4);
         if (a != b) { printf("MISMATCH t=%d n=%zu\n", t, n); return 1; }
+        // raw pointers, as the pore stage sorts a page-locked buffer; level 0 is std::sort's own steps
+        pma::ordered_sort(c.data(), c.data() + c.size(), less, t % 5);
+        if (a != c) { printf("MISMATCH (pointers) t=%d n=%zu\n", t, n); return 1; }
     }
     printf("ok\n");
     return 0;
