@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(256) stream_copy16(const uint4* __restrict__ s
 void* mapped_address(const void* host) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-        (void)cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+        (void)cudaGetLastError();  // an unknown pointer leaves a (non-sticky) error: clear it
         return nullptr;
     }
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
