@@ -2001,18 +2001,41 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
     for (size_t i = 0; i < nt; ++i) by_id[i] = static_cast<uint32_t>(i);
     auto id_less = [&](uint32_t a, uint32_t b) { return t->throats[a].id < t->throats[b].id; };
     if (!std::is_sorted(by_id.begin(), by_id.end(), id_less)) std::sort(by_id.begin(), by_id.end(), id_less);
+    // On host threads when there are many types: a count pass, then the lists written in place.
     std::vector<uint32_t> lists;
-    lists.reserve(t->pool.size());
     std::vector<size_t> loff(nt + 1, 0);
-    std::vector<uint32_t> tmp;
-    for (size_t k = 0; k < nt; ++k) {
-        const pma_throat& th = t->throats[by_id[k]];
-        tmp.assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
-        if (!std::is_sorted(tmp.begin(), tmp.end())) std::sort(tmp.begin(), tmp.end());
-        for (uint32_t pid : tmp)
-            if (pid > max_pore || !is_empty[pid]) lists.push_back(pid);
-        loff[k + 1] = lists.size();
-    }
+    auto filter = [&](size_t lo, size_t hi, bool write) {
+        std::vector<uint32_t> tmp;
+        for (size_t k = lo; k < hi; ++k) {
+            const pma_throat& th = t->throats[by_id[k]];
+            tmp.assign(t->pool.begin() + th.pool_offset, t->pool.begin() + th.pool_offset + th.n_pores);
+            if (!std::is_sorted(tmp.begin(), tmp.end())) std::sort(tmp.begin(), tmp.end());
+            size_t at = write ? loff[k] : 0;
+            for (uint32_t pid : tmp)
+                if (pid > max_pore || !is_empty[pid]) {
+                    if (write) lists[at] = pid;
+                    ++at;
+                }
+            if (!write) loff[k + 1] = at;
+        }
+    };
+    const unsigned nth = nt >= (1u << 15) ? std::max(1u, std::min(8u, std::thread::hardware_concurrency())) : 1u;
+    auto parallel = [&](bool write) {
+        std::vector<std::thread> ts;
+        for (unsigned i = 1; i < nth; ++i) {
+            try {
+                ts.emplace_back(filter, nt * i / nth, nt * (i + 1) / nth, write);
+            } catch (const std::system_error&) {
+                filter(nt * i / nth, nt * (i + 1) / nth, write);  // no thread to be had: in line
+            }
+        }
+        filter(0, nt / nth, write);
+        for (auto& th : ts) th.join();
+    };
+    parallel(false);  // loff[k + 1] = kept length of type k
+    for (size_t k = 0; k < nt; ++k) loff[k + 1] += loff[k];
+    lists.resize(loff[nt]);
+    parallel(true);
     auto len = [&](size_t k) { return loff[k + 1] - loff[k]; };
     phase("removal.filter_ms");
     ctx->count("removal.types", static_cast<double>(nt));
