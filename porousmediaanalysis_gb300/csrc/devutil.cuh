@@ -169,11 +169,12 @@ inline std::vector<uint32_t> pore_id_sequence(size_t n) {
 // the read does not queue on a copy engine behind large transfers of other streams (the
 // pipeline's side-stream result copies), and one launch covers several sources.
 struct ReadBack {
-    const void* src[4];
-    void* dst[4];
-    unsigned words[4];  // 4-byte words
+    const void* src[4] = {};
+    void* dst[4] = {};
+    unsigned words[4] = {};  // 4-byte words
     int n = 0;
     void add(void* host_dst, const void* dev_src, size_t bytes) {
+        PMA_REQUIRE(n < 4, PMA_ERR_INTERNAL, "read-back of more than four arrays");
         src[n] = dev_src;
         dst[n] = host_dst;
         words[n] = static_cast<unsigned>(bytes / 4);
