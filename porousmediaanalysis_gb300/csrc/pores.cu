@@ -2054,13 +2054,29 @@ void remove_empty_pores(pma_ctx* ctx, pma_table* t, uint32_t* labels, pma_dims d
         return len(a) == len(b) && std::equal(lists.begin() + loff[a], lists.begin() + loff[a + 1],
                                               lists.begin() + loff[b]);
     };
-    std::vector<std::pair<unsigned long long, uint32_t>> live;  // (hash of the list, type)
-    for (size_t k = 0; k < nt; ++k) {
-        if (!alive[k]) continue;
-        unsigned long long h = 1469598103934665603ull ^ len(k);
-        for (size_t i = loff[k]; i < loff[k + 1]; ++i) h = (h ^ lists[i]) * 1099511628211ull;
-        live.emplace_back(h, static_cast<uint32_t>(k));
+    std::vector<unsigned long long> lhash(nt);  // hashes of the lists, on the filter's threads
+    auto hash_range = [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; ++k) {
+            unsigned long long h = 1469598103934665603ull ^ len(k);
+            for (size_t i = loff[k]; i < loff[k + 1]; ++i) h = (h ^ lists[i]) * 1099511628211ull;
+            lhash[k] = h;
+        }
+    };
+    {
+        std::vector<std::thread> ts;
+        for (unsigned i = 1; i < nth; ++i) {
+            try {
+                ts.emplace_back(hash_range, nt * i / nth, nt * (i + 1) / nth);
+            } catch (const std::system_error&) {
+                hash_range(nt * i / nth, nt * (i + 1) / nth);  // no thread to be had: in line
+            }
+        }
+        hash_range(0, nt / nth);
+        for (auto& th : ts) th.join();
     }
+    std::vector<std::pair<unsigned long long, uint32_t>> live;  // (hash of the list, type)
+    for (size_t k = 0; k < nt; ++k)
+        if (alive[k]) live.emplace_back(lhash[k], static_cast<uint32_t>(k));
     std::sort(live.begin(), live.end());
     std::vector<uint32_t> members;
     for (size_t i = 0; i < live.size();) {
